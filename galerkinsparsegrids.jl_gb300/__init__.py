@@ -1,0 +1,456 @@
+"""GalerkinSparseGrids.jl's derivative-operator / RK time-stepping path on one
+GB300, behind the reference's API.
+
+Names, argument meaning and errors follow src/GalerkinSparseGrids.jl's exports
+(get_size, V2Dref, D2Vref, vcoeffs_DG, tensor_construct, D_matrix,
+grad_matrix, laplacian_matrix, wave_evolve) so code written against the
+reference reads the same.  Coefficient vectors use the reference's layout
+unchanged.  All compute runs in libsgdg.so (hand-written sm_103a CUDA); there
+is no CPU fallback: without the library or a GPU every compute call raises.
+
+Host-side helpers here (coefficient projection, index maps, sparse exports)
+are set-up and I/O around the hot path, like the reference's own set-up code.
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from ._lib import SGDGError, check, lib
+
+__all__ = [
+    "get_size", "index_map", "V2Dref", "D2Vref", "V2D", "D2V", "dg_coeffs", "vcoeffs_DG", "vcoeffs_1d",
+    "tensor_construct", "fourier_coeffs", "periodic_DLF_matrix", "D_matrix", "grad_matrix", "laplacian_matrix",
+    "SparseGridOperator", "wave_evolve", "advect_evolve", "energy_func", "Batch", "SGDGError", "set_hbm_budget",
+    "hbm_in_use",
+]
+
+
+def _scheme(scheme):
+    if scheme not in _lib.SCHEMES:
+        raise ValueError("scheme must be \"sparse\" or \"full\"")
+    return _lib.SCHEMES[scheme]
+
+
+def _method(method):
+    if method not in _lib.METHODS:
+        raise ValueError("method must be \"plain\" or \"matfree\"")
+    return _lib.METHODS[method]
+
+
+# ---------------------------------------------------------------- layout ----
+def get_size(D, k, n, scheme="sparse"):
+    """Number of coefficients (src/dg_vmethods.jl:179-189)."""
+    N = ctypes.c_int64()
+    check(lib().sgdg_get_size(D, k, n, _scheme(scheme), ctypes.byref(N)))
+    return N.value
+
+
+def index_map(D, k, n, scheme="sparse"):
+    """(level, cell, mode) of every coefficient as three (N, D) int32 arrays, 1-based."""
+    N = get_size(D, k, n, scheme)
+    L = np.zeros(N * D, np.int32)
+    C = np.zeros(N * D, np.int32)
+    M = np.zeros(N * D, np.int32)
+    check(lib().sgdg_index_map(D, k, n, _scheme(scheme), L, C, M))
+    return L.reshape(N, D), C.reshape(N, D), M.reshape(N, D)
+
+
+def V2Dref(D, k, n, scheme="sparse"):
+    """Vector of (level, cell, mode) tuples (src/dg_vmethods.jl:267-286)."""
+    L, C, M = index_map(D, k, n, scheme)
+    return [(tuple(L[i]), tuple(C[i]), tuple(M[i])) for i in range(L.shape[0])]
+
+
+def D2Vref(D, k, n, scheme="sparse"):
+    """Dict (level, cell, mode) -> 1-based vector index (src/dg_vmethods.jl:246-265)."""
+    return {t: i + 1 for i, t in enumerate(V2Dref(D, k, n, scheme))}
+
+
+def V2D(D, k, n, vect, scheme="sparse"):
+    """Vector -> {level: {cell: {mode: value}}} (src/dg_vmethods.jl:220-244)."""
+    out = {}
+    for (lv, cl, md), val in zip(V2Dref(D, k, n, scheme), vect):
+        out.setdefault(lv, {}).setdefault(cl, {})[md] = val
+    return out
+
+
+def D2V(D, k, n, coeffs, scheme="sparse"):
+    """Inverse of V2D (src/dg_vmethods.jl:192-217)."""
+    return np.array([coeffs[lv][cl][md] for (lv, cl, md) in V2Dref(D, k, n, scheme)])
+
+
+def dg_coeffs(k):
+    """dg_coeffs[k] (src/1d_dg_functions.jl:243-253) as a (2k, k) array."""
+    out = np.zeros(2 * k * k)
+    check(lib().sgdg_dg_coeffs(k, out))
+    return out.reshape(k, 2 * k).T.copy()
+
+
+# ------------------------------------------------------------ projection ----
+def _legendre_monomials(m):
+    """Orthonormal Legendre polynomial of degree m on [-1,1], monomial coefficients."""
+    c = np.polynomial.legendre.leg2poly(np.eye(m + 1)[m])
+    return c * np.sqrt((2 * m + 1) / 2.0)
+
+
+def _eval_v(k, lvl, cell, mode, x):
+    """Hierarchical basis function v (src/dg_methods.jl:27-36) at points x (vectorised)."""
+    x = np.asarray(x, np.float64)
+    if lvl == 0:
+        p = _legendre_monomials(mode - 1)
+        return np.sqrt(2.0) * np.polynomial.polynomial.polyval(2 * x - 1, p) * ((x >= 0) & (x <= 1))
+    y = (1 << lvl) * x - (2 * cell - 1)
+    c = dg_coeffs(k)[:, mode - 1]
+    a, b = c[:k], c[k:]
+    val = np.polynomial.polynomial.polyval(y, a) + np.sign(y) * np.polynomial.polynomial.polyval(y, b)
+    return np.sqrt(float(1 << lvl)) * val * (np.abs(y) <= 1)
+
+
+def _pieces_1d(k, n, q, hmax=1.0 / 16):
+    """Per 1D block: quadrature nodes/weights on its polynomial pieces (split
+    further into sub-intervals no wider than hmax) and the basis values there.
+    Returns list over levels L=1..n+1 of arrays nodes (cells, P),
+    weights (P,), values (cells, k, P)."""
+    gx, gw = np.polynomial.legendre.leggauss(q)
+    out = []
+    for L in range(1, n + 2):
+        lvl = L - 1
+        nc = 1 << max(0, L - 2)
+        w = 1.0 / (1 << max(0, lvl - 1))
+        halves = 1 if lvl == 0 else 2
+        sub = max(1, int(np.ceil(w / halves / hmax - 1e-12)))
+        parts = halves * sub  # sub-intervals per cell, never straddling the midpoint
+        loc = np.concatenate([(h + 0.5 + 0.5 * gx) / parts for h in range(parts)])  # in [0,1] of the cell
+        wts = np.concatenate([0.5 * gw / parts for _ in range(parts)]) * w
+        nodes = (np.arange(nc)[:, None] + loc[None, :]) * w
+        vals = np.stack([np.stack([_eval_v(k, lvl, c + 1, m, nodes[c]) for m in range(1, k + 1)])
+                         for c in range(nc)])
+        out.append((nodes, wts, vals))
+    return out
+
+
+def vcoeffs_1d(k, n, f, q=None):
+    """1D hierarchical coefficients of a vectorised f (1D vector order)."""
+    q = q or max(8, k + 4)
+    res = []
+    for nodes, wts, vals in _pieces_1d(k, n, q):
+        res.append(np.einsum("cmp,cp,p->cm", vals, f(nodes), wts).ravel())
+    return np.concatenate(res)
+
+
+def vcoeffs_DG(D, k, n, f, scheme="sparse", q=None):
+    """Coefficient vector of f (src/dg_vmethods.jl:293-323).
+
+    ``f`` takes an (npts, D) array of points and returns npts values.  The
+    reference integrates each basis function with hcubature; here every level
+    block is integrated at once with tensor Gauss-Legendre rules on the
+    polynomial pieces (exact for polynomials of degree < 2q)."""
+    q = q or max(6, k + 3)
+    if D == 1:
+        return vcoeffs_1d(k, n, lambda x: np.asarray(f(x.reshape(-1, 1)), np.float64).reshape(x.shape), q)
+    pieces = _pieces_1d(k, n, q)
+    L, _, _ = index_map(D, k, n, scheme)
+    N = L.shape[0]
+    out = np.empty(N)
+    lv_rows = {}
+    pos = 0
+    while pos < N:
+        lv = tuple(L[pos])
+        cells = [1 << max(0, l - 2) for l in lv]
+        size = int(np.prod(cells)) * k ** D
+        lv_rows[lv] = (pos, size)
+        pos += size
+    for lv, (pos, size) in lv_rows.items():
+        nodes = [pieces[l - 1][0] for l in lv]  # (cells_q, P_q)
+        grids = np.meshgrid(*[nd.ravel() for nd in nodes], indexing="ij")
+        pts = np.stack([g.ravel() for g in grids], axis=1)
+        F = np.asarray(f(pts), np.float64).reshape([nd.size for nd in nodes])
+        shape = []
+        for nd in nodes:
+            shape += [nd.shape[0], nd.shape[1]]
+        F = F.reshape(shape)  # (c1, p1, c2, p2, ...)
+        for qd, l in enumerate(lv):
+            _, wts, vals = pieces[l - 1]
+            W = vals * wts[None, None, :]  # (c, m, p)
+            # contract axis pair (c_q, p_q) currently at positions (2q, 2q+1) -> (c_q, m_q)
+            F = np.moveaxis(F, (2 * qd, 2 * qd + 1), (0, 1))
+            F = np.einsum("cp...,cmp->cm...", F, W)
+            F = np.moveaxis(F, (0, 1), (2 * qd, 2 * qd + 1))
+        # axes (c1, m1, ..., cD, mD) -> reference order: cells (dim 1 fastest) then modes (dim 1 fastest)
+        order = [2 * q for q in reversed(range(D))] + [2 * q + 1 for q in reversed(range(D))]
+        out[pos:pos + size] = np.transpose(F, order).ravel()
+    return out
+
+
+def _i1d(k, L, C, M):
+    start = np.where(L >= 2, 1 << np.maximum(L - 2, 0), 0)
+    return k * (start + C - 1) + M - 1
+
+
+def tensor_construct(D, k, n, vcoeff_array, scheme="sparse"):
+    """Coefficients of prod_d f_d(x_d) from 1D coefficient vectors
+    (src/tensor_construct.jl:323-329)."""
+    L, C, M = index_map(D, k, n, scheme)
+    out = np.ones(L.shape[0])
+    for q in range(D):
+        out *= np.asarray(vcoeff_array[q], np.float64)[_i1d(k, L[:, q], C[:, q], M[:, q])]
+    return out
+
+
+def fourier_coeffs(D, k, n, modes, scheme="sparse"):
+    """Coefficients of sum_m amp * trig(2 pi a.x + phase), exactly separable:
+    ``modes`` = [(a (D ints), amp, "sin"|"cos", phase), ...]."""
+    L, C, M = index_map(D, k, n, scheme)
+    idx = [_i1d(k, L[:, q], C[:, q], M[:, q]) for q in range(D)]
+    cache = {}
+
+    def e1d(a):
+        if a not in cache:
+            re = vcoeffs_1d(k, n, lambda x: np.cos(2 * np.pi * a * x), q=max(12, k + 8))
+            im = vcoeffs_1d(k, n, lambda x: np.sin(2 * np.pi * a * x), q=max(12, k + 8))
+            cache[a] = re + 1j * im
+        return cache[a]
+
+    out = np.zeros(L.shape[0])
+    for a, amp, kind, ph in modes:
+        z = np.exp(1j * ph) * np.ones(L.shape[0], complex)
+        for q in range(D):
+            z *= e1d(int(a[q]))[idx[q]]
+        out += amp * (z.real if kind == "cos" else z.imag)
+    return out
+
+
+# ------------------------------------------------------------- operators ----
+def _csr_from(nnz_fn, export_fn, m):
+    nnz = ctypes.c_int64()
+    check(nnz_fn(ctypes.byref(nnz)))
+    rp = np.zeros(m + 1, np.int64)
+    col = np.zeros(max(nnz.value, 1), np.int32)
+    val = np.zeros(max(nnz.value, 1), np.float64)
+    check(export_fn(rp, col, val))
+    return sp.csr_matrix((val[:nnz.value], col[:nnz.value], rp), shape=(m, m))
+
+
+def periodic_DLF_matrix(k, n):
+    """1D hierarchical periodic DG derivative (src/1d_derivative.jl:136-148), CSR."""
+    L = lib()
+    return _csr_from(lambda p: L.sgdg_dlf_1d_nnz(k, n, p), lambda a, b, c: L.sgdg_dlf_1d_export(k, n, a, b, c),
+                     k << n)
+
+
+class SparseGridOperator:
+    """Device-backed derivative operators for one (D, k, n, scheme)."""
+
+    def __init__(self, D, k, n, scheme="sparse"):
+        self.D, self.k, self.n, self.scheme = D, k, n, scheme
+        h = ctypes.c_void_p()
+        check(lib().sgdg_op_create(D, k, n, _scheme(scheme), ctypes.byref(h)))
+        self._h = h
+        self.N = get_size(D, k, n, scheme)
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sgdg_op_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _len(self, which):
+        return 2 * self.N if which == _lib.OP_WAVE_RHS else self.N
+
+    def nnz(self, which):
+        z = ctypes.c_int64()
+        check(lib().sgdg_op_nnz(self._h, which, ctypes.byref(z)))
+        return z.value
+
+    def csr(self, which):
+        """The assembled operator as scipy CSR (numerical zeros stored like the reference)."""
+        m = self._len(which)
+        return _csr_from(lambda p: lib().sgdg_op_nnz(self._h, which, p),
+                         lambda a, b, c: lib().sgdg_op_export_csr(self._h, which, a, b, c), m)
+
+    def apply(self, x, which=1, method="plain"):
+        """y = A x on the GPU (host arrays in and out)."""
+        x = np.ascontiguousarray(x, np.float64)
+        if x.shape != (self._len(which),):
+            raise ValueError("x must have %d entries" % self._len(which))
+        y = np.empty_like(x)
+        check(lib().sgdg_apply(self._h, which, _method(method), x, y))
+        return y
+
+    def apply_device(self, x_ptr, y_ptr, which=1, method="plain", stream=0):
+        check(lib().sgdg_apply_device(self._h, which, _method(method), ctypes.c_void_p(x_ptr),
+                                      ctypes.c_void_p(y_ptr), ctypes.c_void_p(stream)))
+
+
+def D_matrix(D, d, k, n, scheme="sparse"):
+    """D-dimensional derivative along dim d, 1-based (src/multidim_derivative.jl:209-213)."""
+    return SparseGridOperator(D, k, n, scheme).csr(d)
+
+
+def grad_matrix(D, k, n, scheme="sparse"):
+    op = SparseGridOperator(D, k, n, scheme)
+    return [op.csr(d) for d in range(1, D + 1)]
+
+
+def laplacian_matrix(D, k, n, scheme="sparse"):
+    return SparseGridOperator(D, k, n, scheme).csr(_lib.OP_LAPLACIAN)
+
+
+# -------------------------------------------------------------- evolvers ----
+def _steps(t0, t1, dt, nsteps):
+    if nsteps is None:
+        if dt is None:
+            raise ValueError("give dt or nsteps (fixed-step classical RK4)")
+        nsteps = int(round((t1 - t0) / dt))
+        if nsteps < 1 or abs(nsteps * dt - (t1 - t0)) > 1e-9 * max(1.0, abs(t1 - t0)):
+            raise ValueError("(t1 - t0) must be a whole number of steps dt")
+    return int(nsteps)
+
+
+def _order(order):
+    if order != "rk4":
+        # the reference accepts "45"/"78" (ODE.jl adaptive) and throws
+        # ArgumentError(:order) otherwise (src/pdes.jl:62-68)
+        raise ValueError("order: only fixed-step classical \"rk4\" is implemented on the GPU")
+
+
+def wave_evolve(D, k, n, f0, v0, time0, time1, order="rk4", scheme="sparse", dt=None, nsteps=None, nout=2,
+                method="plain", op=None):
+    """u_tt = laplacian(u) on the periodic unit cube (src/pdes.jl:54-83).
+
+    Returns (times, states): nout equally spaced states [f; v] of length 2N.
+    f0, v0 are coefficient vectors or functions (projected with vcoeffs_DG)."""
+    _order(order)
+    if callable(f0):
+        f0 = vcoeffs_DG(D, k, n, f0, scheme)
+    if callable(v0):
+        v0 = vcoeffs_DG(D, k, n, v0, scheme)
+    op = op or SparseGridOperator(D, k, n, scheme)
+    f0 = np.ascontiguousarray(f0, np.float64)
+    v0 = np.ascontiguousarray(v0, np.float64)
+    if f0.shape != (op.N,) or v0.shape != (op.N,):
+        raise ValueError("f0 and v0 must have get_size(D,k,n) = %d entries" % op.N)
+    ns = _steps(time0, time1, dt, nsteps)
+    times = np.zeros(nout)
+    states = np.zeros((nout, 2 * op.N))
+    check(lib().sgdg_wave_evolve(op._h, f0, v0, float(time0), float(time1), ns, int(nout), _method(method), times,
+                                 states.reshape(-1)))
+    return times, list(states)
+
+
+def advect_evolve(D, k, n, a, f0, time0, time1, order="rk4", scheme="sparse", dt=None, nsteps=None, nout=2,
+                  method="plain", op=None):
+    """f_t = -sum_d a_d D_d f on the periodic unit cube (operator composed
+    from grad_matrix, src/multidim_derivative.jl:215-217).  Returns (times, states)."""
+    _order(order)
+    if callable(f0):
+        f0 = vcoeffs_DG(D, k, n, f0, scheme)
+    op = op or SparseGridOperator(D, k, n, scheme)
+    a = np.ascontiguousarray(a, np.float64)
+    f0 = np.ascontiguousarray(f0, np.float64)
+    if a.shape != (D,):
+        raise ValueError("a must have D entries")
+    if f0.shape != (op.N,):
+        raise ValueError("f0 must have get_size(D,k,n) = %d entries" % op.N)
+    ns = _steps(time0, time1, dt, nsteps)
+    times = np.zeros(nout)
+    states = np.zeros((nout, op.N))
+    check(lib().sgdg_advect_evolve(op._h, a, f0, float(time0), float(time1), ns, int(nout), _method(method), times,
+                                   states.reshape(-1)))
+    return times, list(states)
+
+
+def energy_func(D, k, n, soln, scheme="sparse", op=None):
+    """sum_d ||D_d u||^2 + ||u_t||^2 per stored state (src/pdes.jl:258-273), D_d applied on the GPU."""
+    op = op or SparseGridOperator(D, k, n, scheme)
+    times, states = soln
+    N = op.N
+    energies = []
+    for s in states:
+        s = np.asarray(s, np.float64)
+        u, ut = s[:N], s[N:]
+        energies.append(sum(float(np.sum(op.apply(u, d) ** 2)) for d in range(1, D + 1)) + float(np.sum(ut ** 2)))
+    return np.array(times), np.array(energies)
+
+
+# --------------------------------------------------------------- batches ----
+class Batch:
+    """Independent solves of uneven (D, k, n) advanced together by the
+    matrix-free FP32/FP64 engine (one launch per dimension per RK stage,
+    replayed from a CUDA graph)."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().sgdg_batch_create(ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sgdg_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, kind, D, k, n, y0, dt, a=None, scheme="sparse"):
+        kinds = {"advect": _lib.KIND_ADVECT, "wave": _lib.KIND_WAVE}
+        if kind not in kinds:
+            raise ValueError("kind must be \"advect\" or \"wave\"")
+        y0 = np.ascontiguousarray(y0, np.float64)
+        ap = None
+        if a is not None:
+            a_arr = np.ascontiguousarray(a, np.float64)
+            ap = a_arr.ctypes.data_as(ctypes.c_void_p)
+        i = ctypes.c_int()
+        check(lib().sgdg_batch_add(self._h, kinds[kind], D, k, n, _scheme(scheme), ap, float(dt), y0,
+                                   ctypes.byref(i)))
+        return i.value
+
+    def remove(self, sid):
+        check(lib().sgdg_batch_remove(self._h, sid))
+
+    def set_stream(self, stream):
+        check(lib().sgdg_batch_set_stream(self._h, ctypes.c_void_p(stream)))
+
+    def step(self, nsteps=1):
+        check(lib().sgdg_batch_step(self._h, int(nsteps)))
+
+    def state_size(self, sid):
+        z = ctypes.c_int64()
+        check(lib().sgdg_batch_state_size(self._h, sid, ctypes.byref(z)))
+        return z.value
+
+    def state(self, sid):
+        y = np.empty(self.state_size(sid))
+        check(lib().sgdg_batch_get_state(self._h, sid, y))
+        return y
+
+    def step_info(self):
+        launches = ctypes.c_int64()
+        dofs = ctypes.c_double()
+        check(lib().sgdg_batch_step_info(self._h, ctypes.byref(launches), ctypes.byref(dofs)))
+        return launches.value, dofs.value
+
+
+def set_hbm_budget(nbytes):
+    check(lib().sgdg_set_hbm_budget(int(nbytes)))
+
+
+def hbm_in_use():
+    z = ctypes.c_int64()
+    check(lib().sgdg_hbm_in_use(ctypes.byref(z)))
+    return z.value
+
+
+def sync():
+    check(lib().sgdg_sync())

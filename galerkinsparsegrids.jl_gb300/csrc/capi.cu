@@ -1,0 +1,932 @@
+// capi.cu -- the C ABI of libsgdg (include/sgdg.h) and its host drivers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sgdg.h"
+#include "engine.h"
+#include "sgdg_core.h"
+
+namespace sgdg {
+
+cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st);
+cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
+                           int stage, cudaStream_t st);
+cudaError_t launch_mf_pass(const MFTile* tiles, int ntiles, const MFSolve* solves, int stage, int in_sel, int rk,
+                           size_t smem, int grid, cudaStream_t st);
+cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
+cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            throw Error(e_ == cudaErrorMemoryAllocation ? SGDG_ENOMEM_BUDGET : SGDG_ECUDA,             \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+    } while (0)
+
+// ------------------------------------------------------------ device ----
+static void require_gpu() {
+    static int state = -1;  // -1 unknown, 0 none, 1 ok
+    if (state == 1) return;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        state = 0;
+        throw Error(SGDG_ENOGPU, std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
+    }
+    state = 1;
+}
+
+static std::atomic<int64_t> g_budget{0}, g_in_use{0};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t n) { alloc(n); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        release();
+        p = o.p;
+        bytes = o.bytes;
+        o.p = nullptr;
+        o.bytes = 0;
+        return *this;
+    }
+    void alloc(size_t n) {
+        release();
+        if (n == 0) n = 16;
+        int64_t b = g_budget.load();
+        if (b > 0 && g_in_use.load() + (int64_t)n > b)
+            throw Error(SGDG_ENOMEM_BUDGET, "HBM budget exceeded: requested " + std::to_string(n) + " bytes, " +
+                                                std::to_string(g_in_use.load()) + " of " + std::to_string(b) + " in use");
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            throw Error(SGDG_ENOMEM_BUDGET, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        bytes = n;
+        g_in_use += (int64_t)n;
+    }
+    void release() {
+        if (p) {
+            cudaFree(p);
+            g_in_use -= (int64_t)bytes;
+        }
+        p = nullptr;
+        bytes = 0;
+    }
+    ~DevBuf() { release(); }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+template <class T>
+static DevBuf upload(const std::vector<T>& v, cudaStream_t st) {
+    DevBuf b(v.size() * sizeof(T));
+    if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return b;
+}
+
+// ------------------------------------------------------- plain form ----
+struct DeviceCSR {
+    DevBuf rowptr, col, val;
+    DevCSR d{};
+};
+
+static int pick_vs(const CSR& A) {
+    double avg = A.m ? double(A.nnz()) / double(A.m) : 0.0;
+    if (avg <= 2) return 1;
+    if (avg <= 4) return 2;
+    if (avg <= 10) return 4;
+    if (avg <= 24) return 8;
+    if (avg <= 48) return 16;
+    return 32;
+}
+
+static std::unique_ptr<DeviceCSR> to_device(const CSR& A, cudaStream_t st) {
+    auto D = std::make_unique<DeviceCSR>();
+    D->rowptr = upload(A.rowptr, st);
+    D->col = upload(A.col, st);
+    D->val = upload(A.val, st);
+    D->d.m = A.m;
+    D->d.nnz = A.nnz();
+    D->d.rowptr = D->rowptr.as<int64_t>();
+    D->d.col = D->col.as<int32_t>();
+    D->d.val = D->val.as<double>();
+    D->d.vs = pick_vs(A);
+    return D;
+}
+
+// ------------------------------------------------- matrix-free engine ----
+struct SolveSpec {
+    int kind, D, k, n, scheme;
+    double a[8];
+    double dt;
+    int apply_dim;  // -1: all dimensions; else only this 0-based dimension (apply mode)
+};
+
+struct STable {  // 1D operator in FP32 block CSR on the device
+    DevBuf rowptr, colblk, val;
+};
+
+struct SolveState {
+    SolveSpec spec;
+    SparseIndex ix;
+    int64_t N = 0, Ns = 0;
+    DevBuf y, acc, u0, u1, rhs, boff;
+    std::vector<int64_t> boff_h;
+    std::vector<MFTile> tiles;  // solve index filled at plan time
+    bool live = true;
+};
+
+static constexpr int kTileElems = 4096;
+
+class MFEngine {
+   public:
+    explicit MFEngine(cudaStream_t st = nullptr) : stream_(st) {}
+    ~MFEngine() { drop_graph(); }
+
+    void set_stream(cudaStream_t st) {
+        if (st != stream_) drop_graph();
+        stream_ = st;
+    }
+    cudaStream_t stream() const { return stream_; }
+
+    int add(const SolveSpec& sp, const double* y0_host, bool y0_device = false) {
+        require_gpu();
+        auto s = std::make_unique<SolveState>();
+        s->spec = sp;
+        s->ix = make_index(sp.D, sp.k, sp.n, sp.scheme);
+        if (sp.k > 5) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports k <= 5 (use the plain form)");
+        auto op = dlf1d(sp.k, sp.n);
+        stab(sp.k, sp.n, *op);
+        s->N = s->ix.N;
+        s->Ns = sp.kind == MF_KIND_WAVE ? 2 * s->N : s->N;
+        // pencils and tiles
+        for (int d = 0; d < sp.D; d++) {
+            if (sp.apply_dim >= 0 && d != sp.apply_dim) continue;
+            auto pens = make_pencils(s->ix, d);
+            int kd1 = 1, kDm1 = 1;
+            for (int q = 0; q < d; q++) kd1 *= sp.k;
+            for (int q = 0; q < sp.D - 1; q++) kDm1 *= sp.k;
+            for (const auto& p : pens) {
+                int32_t boff = (int32_t)s->boff_h.size();
+                for (auto o : p.blockoff) s->boff_h.push_back(o);
+                int64_t m = int64_t(sp.k) << (p.lmax - 1);
+                int64_t wc = std::max<int64_t>(1, std::min<int64_t>(p.R, kTileElems / m));
+                for (int64_t r0 = 0; r0 < p.R; r0 += wc) {
+                    MFTile t{};
+                    t.d = (int16_t)d;
+                    int first_d = sp.apply_dim >= 0 ? sp.apply_dim : 0;
+                    int last_d = sp.apply_dim >= 0 ? sp.apply_dim : sp.D - 1;
+                    t.flags = (int16_t)((d == first_d ? TILE_FIRST : 0) | (d == last_d ? TILE_LAST : 0));
+                    t.lmax = p.lmax;
+                    t.lp = p.lp;
+                    t.boff = boff;
+                    t.r0 = (int32_t)r0;
+                    t.wc = (int32_t)std::min<int64_t>(wc, p.R - r0);
+                    t.kd1 = kd1;
+                    t.kDm1 = kDm1;
+                    s->tiles.push_back(t);
+                }
+            }
+        }
+        s->y.alloc(sizeof(double) * s->Ns);
+        s->acc.alloc(sizeof(double) * s->Ns);
+        s->u0.alloc(sizeof(float) * s->Ns);
+        s->u1.alloc(sizeof(float) * s->Ns);
+        s->rhs.alloc(sizeof(float) * s->N);
+        s->boff = upload(s->boff_h, stream_);
+        if (y0_host) {
+            if (y0_device)
+                CK(cudaMemcpyAsync(s->y.p, y0_host, sizeof(double) * s->Ns, cudaMemcpyDeviceToDevice, stream_));
+            else
+                CK(cudaMemcpyAsync(s->y.p, y0_host, sizeof(double) * s->Ns, cudaMemcpyHostToDevice, stream_));
+            CK(launch_f64_to_f32(s->y.as<double>(), s->u0.as<float>(), s->Ns, stream_));
+        }
+        solves_.push_back(std::move(s));
+        dirty_ = true;
+        return (int)solves_.size() - 1;
+    }
+
+    void remove(int id) {
+        SolveState& s = at(id);
+        CK(cudaStreamSynchronize(stream_));
+        s.live = false;
+        s.y.release();
+        s.acc.release();
+        s.u0.release();
+        s.u1.release();
+        s.rhs.release();
+        s.boff.release();
+        s.tiles.clear();
+        dirty_ = true;
+    }
+
+    SolveState& at(int id) {
+        if (id < 0 || id >= (int)solves_.size() || !solves_[id]->live) throw Error(SGDG_EINVAL, "no such solve id");
+        return *solves_[id];
+    }
+
+    // u[0] <- fp32(x) for apply mode (x on device, N values)
+    void load_input_device(int id, const double* x_dev) {
+        SolveState& s = at(id);
+        CK(launch_f64_to_f32(x_dev, s.u0.as<float>(), s.N, stream_));
+    }
+
+    void run_apply(double* y_dev) {
+        plan();
+        for (int p = 0; p < dmax_; p++)
+            CK(launch_mf_pass(tiles_d_.as<MFTile>() + pass_begin_[p], pass_begin_[p + 1] - pass_begin_[p],
+                              solves_d_.as<MFSolve>(), 1, 0, 0, smem_, 0, stream_));
+        SolveState& s = *solves_[0];
+        CK(launch_f32_to_f64(s.rhs.as<float>(), y_dev, s.N, stream_));
+    }
+
+    void step(int64_t nsteps) {
+        plan();
+        if (ntiles_ == 0 || nsteps <= 0) return;
+        if (!graph_) capture();
+        for (int64_t i = 0; i < nsteps; i++) CK(cudaGraphLaunch(graph_, stream_));
+    }
+
+    void get_state(int id, double* host) {
+        SolveState& s = at(id);
+        CK(cudaMemcpyAsync(host, s.y.p, sizeof(double) * s.Ns, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+
+    double dof_updates_per_step() const {
+        double t = 0;
+        for (auto& s : solves_)
+            if (s->live) t += 4.0 * double(s->Ns);
+        return t;
+    }
+    int64_t launches_per_step() const {
+        int dm = 0;
+        for (auto& s : solves_)
+            if (s->live) dm = std::max(dm, s->spec.apply_dim >= 0 ? 1 : s->spec.D);
+        return 4LL * dm;
+    }
+    size_t smem() const { return smem_; }
+
+   private:
+    void stab(int k, int n, const DLF1D& op) {
+        auto key = std::make_pair(k, n);
+        if (stabs_.count(key)) return;
+        const int kk = ((k * k + 3) / 4) * 4;
+        std::vector<float> v((size_t)op.colblk.size() * kk, 0.f);
+        for (size_t b = 0; b < op.colblk.size(); b++)
+            for (int t = 0; t < k * k; t++) v[b * kk + t] = (float)op.val[b * k * k + t];
+        STable S;
+        S.rowptr = upload(op.rowptr, stream_);
+        S.colblk = upload(op.colblk, stream_);
+        S.val = upload(v, stream_);
+        stabs_.emplace(key, std::move(S));
+    }
+
+    void plan() {
+        if (!dirty_) return;
+        drop_graph();
+        std::vector<MFSolve> sh;
+        std::vector<std::vector<MFTile>> per_pass(kDMax);
+        dmax_ = 0;
+        size_t smem = 0;
+        for (size_t i = 0; i < solves_.size(); i++) {
+            SolveState& s = *solves_[i];
+            MFSolve m{};
+            if (s.live) {
+                const STable& S = stabs_.at({s.spec.k, s.spec.n});
+                m.y = s.y.as<double>();
+                m.acc = s.acc.as<double>();
+                m.u[0] = s.u0.as<float>();
+                m.u[1] = s.u1.as<float>();
+                m.rhs = s.rhs.as<float>();
+                m.s_rowptr = S.rowptr.as<int32_t>();
+                m.s_colblk = S.colblk.as<int32_t>();
+                m.s_val = S.val.as<float>();
+                m.blockoff = s.boff.as<int64_t>();
+                m.dt = s.spec.dt;
+                m.N = s.N;
+                m.D = s.spec.D;
+                m.k = s.spec.k;
+                m.kk = ((s.spec.k * s.spec.k + 3) / 4) * 4;
+                m.kind = s.spec.kind;
+                int kD = 1;
+                for (int q = 0; q < s.spec.D; q++) kD *= s.spec.k;
+                m.kD = kD;
+                m.status = 0;
+                for (int d = 0; d < 8; d++)
+                    m.coef[d] = (float)(s.spec.kind == MF_KIND_WAVE ? 1.0 : (s.spec.apply_dim >= 0 ? 1.0 : -s.spec.a[d]));
+                int pass = 0;
+                for (auto t : s.tiles) {
+                    t.solve = (int32_t)i;
+                    pass = s.spec.apply_dim >= 0 ? 0 : t.d;
+                    per_pass[pass].push_back(t);
+                    int64_t mrows = int64_t(s.spec.k) << (t.lmax - 1);
+                    size_t b = 4 * (2 * (size_t)t.wc + (size_t)(mrows * t.wc) * (s.spec.kind == MF_KIND_WAVE ? 2 : 1));
+                    smem = std::max(smem, b);
+                    dmax_ = std::max(dmax_, pass + 1);
+                }
+            } else {
+                m.status = 1;
+            }
+            sh.push_back(m);
+        }
+        if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "pencil tile exceeds shared memory");
+        smem_ = smem;
+        std::vector<MFTile> all;
+        pass_begin_.assign(1, 0);
+        for (int p = 0; p < dmax_; p++) {
+            all.insert(all.end(), per_pass[p].begin(), per_pass[p].end());
+            pass_begin_.push_back((int)all.size());
+        }
+        ntiles_ = (int)all.size();
+        solves_d_ = upload(sh, stream_);
+        tiles_d_ = upload(all, stream_);
+        CK(cudaStreamSynchronize(stream_));
+        dirty_ = false;
+    }
+
+    void capture() {
+        cudaStream_t cs = stream_;
+        cudaStream_t own = nullptr;
+        if (cs == nullptr) {  // graphs cannot be captured on the legacy stream
+            CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+            cs = own;
+        }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        cudaError_t err = cudaSuccess;
+        for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
+            for (int p = 0; p < dmax_ && err == cudaSuccess; p++)
+                err = launch_mf_pass(tiles_d_.as<MFTile>() + pass_begin_[p], pass_begin_[p + 1] - pass_begin_[p],
+                                     solves_d_.as<MFSolve>(), stage, (stage - 1) % 2, 1, smem_, 0, cs);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        if (own) cudaStreamDestroy(own);
+        if (err != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            throw Error(SGDG_ECUDA, std::string("graph capture: ") + cudaGetErrorString(err != cudaSuccess ? err : e2));
+        }
+        cudaError_t e3 = cudaGraphInstantiate(&graph_, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) {
+            graph_ = nullptr;
+            throw Error(SGDG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+        }
+    }
+
+    void drop_graph() {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+
+    cudaStream_t stream_ = nullptr;
+    std::vector<std::unique_ptr<SolveState>> solves_;
+    std::map<std::pair<int, int>, STable> stabs_;
+    DevBuf solves_d_, tiles_d_;
+    std::vector<int> pass_begin_;
+    int dmax_ = 0, ntiles_ = 0;
+    size_t smem_ = 0;
+    bool dirty_ = true;
+    cudaGraphExec_t graph_ = nullptr;
+};
+
+}  // namespace sgdg
+
+using namespace sgdg;
+
+// ------------------------------------------------------------ handles ----
+struct sgdg_op {
+    SparseIndex ix;
+    std::shared_ptr<const DLF1D> dlf;
+    std::vector<std::unique_ptr<CSR>> dd;  // D_d, built on demand
+    std::unique_ptr<CSR> lap, wave;
+    std::map<int, std::unique_ptr<DeviceCSR>> dev;  // plain-form device copies by `which`
+    std::map<int, std::unique_ptr<MFEngine>> mf_apply;
+    cudaStream_t stream = nullptr;
+
+    const CSR& get(int which) {
+        const int D = ix.D;
+        if (which >= 1 && which <= D) {
+            if (!dd[which - 1]) dd[which - 1].reset(new CSR(assemble_dd(ix, *dlf, which - 1)));
+            return *dd[which - 1];
+        }
+        if (which == SGDG_OP_LAPLACIAN || which == SGDG_OP_WAVE_RHS) {
+            if (!lap) {
+                std::vector<const CSR*> v;
+                for (int d = 1; d <= D; d++) v.push_back(&get(d));
+                lap.reset(new CSR(spgemm_sum(v)));
+            }
+            if (which == SGDG_OP_LAPLACIAN) return *lap;
+            if (!wave) wave.reset(new CSR(wave_rhs(*lap)));
+            return *wave;
+        }
+        throw Error(SGDG_EINVAL, "operator selector must be 1..D, 0 (laplacian) or -1 (wave RHS)");
+    }
+    const DevCSR& device(int which) {
+        auto it = dev.find(which);
+        if (it == dev.end()) it = dev.emplace(which, to_device(get(which), stream)).first;
+        return it->second->d;
+    }
+    ~sgdg_op() {
+        dev.clear();
+        mf_apply.clear();
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct sgdg_batch {
+    MFEngine eng;
+    cudaStream_t own = nullptr;
+    ~sgdg_batch() {
+        if (own) cudaStreamDestroy(own);
+    }
+};
+
+#define API_BEGIN try {
+#define API_END                                        \
+    return SGDG_OK;                                    \
+    }                                                  \
+    catch (const sgdg::Error& e) {                     \
+        set_error(e.what());                           \
+        return e.code;                                 \
+    }                                                  \
+    catch (const std::bad_alloc&) {                    \
+        set_error("host allocation failed");           \
+        return SGDG_ENOMEM_BUDGET;                     \
+    }                                                  \
+    catch (const std::exception& e) {                  \
+        set_error(e.what());                           \
+        return SGDG_EINVAL;                            \
+    }
+
+#define NEED(p)                                                    \
+    do {                                                           \
+        if (!(p)) throw Error(SGDG_EINVAL, #p " must not be NULL"); \
+    } while (0)
+
+static void copy_str(const std::string& s, char* buf, size_t len) {
+    if (!buf || len == 0) return;
+    size_t n = std::min(len - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
+}
+
+static cudaStream_t op_stream(sgdg_op* op) {
+    require_gpu();
+    if (!op->stream) CK(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+    return op->stream;
+}
+
+extern "C" {
+
+int sgdg_version(char* buf, size_t len) {
+    copy_str("sgdg 0.1 (sm_103a)", buf, len);
+    return SGDG_OK;
+}
+
+int sgdg_last_error(char* buf, size_t len) {
+    copy_str(g_err, buf, len);
+    return SGDG_OK;
+}
+
+int sgdg_get_size(int D, int k, int n, int scheme, int64_t* N) {
+    API_BEGIN
+    NEED(N);
+    *N = make_index(D, k, n, scheme).N;
+    API_END
+}
+
+int sgdg_index_map(int D, int k, int n, int scheme, int32_t* level, int32_t* cell, int32_t* mode) {
+    API_BEGIN
+    NEED(level);
+    NEED(cell);
+    NEED(mode);
+    SparseIndex ix = make_index(D, k, n, scheme);
+    int64_t j = 0;
+    for (int b = 0; b < ix.nlev; b++) {
+        const int* L = &ix.levels[(size_t)b * D];
+        for (int64_t cl = 0; cl < ix.lev_cells[b]; cl++)
+            for (int64_t ml = 0; ml < ix.kD; ml++) {
+                int64_t c = cl, m = ml;
+                for (int q = 0; q < D; q++) {
+                    level[j * D + q] = L[q];
+                    int64_t nc = ncells(L[q]);
+                    cell[j * D + q] = int32_t(c % nc) + 1;
+                    c /= nc;
+                    mode[j * D + q] = int32_t(m % k) + 1;
+                    m /= k;
+                }
+                j++;
+            }
+    }
+    API_END
+}
+
+int sgdg_dg_coeffs(int k, double* out) {
+    API_BEGIN
+    NEED(out);
+    const Basis1D& B = basis(k);
+    std::memcpy(out, B.dg.data(), sizeof(double) * B.dg.size());
+    API_END
+}
+
+static CSR dlf_csr(int k, int n) {
+    auto op = dlf1d(k, n);
+    CSR A;
+    A.m = A.n = int64_t(k) << n;
+    A.rowptr.assign(A.m + 1, 0);
+    for (int rb = 0; rb < op->nblocks; rb++)
+        for (int i = 0; i < k; i++) {
+            int64_t row = (int64_t)rb * k + i;
+            for (int p = op->rowptr[rb]; p < op->rowptr[rb + 1]; p++)
+                for (int j = 0; j < k; j++) {
+                    A.col.push_back(op->colblk[p] * k + j);
+                    A.val.push_back(op->val[(size_t)p * k * k + i * k + j]);
+                }
+            A.rowptr[row + 1] = (int64_t)A.col.size();
+        }
+    return A;
+}
+
+int sgdg_dlf_1d_nnz(int k, int n, int64_t* nnz) {
+    API_BEGIN
+    NEED(nnz);
+    basis(k);
+    auto op = dlf1d(k, n);
+    *nnz = (int64_t)op->colblk.size() * k * k;
+    API_END
+}
+
+int sgdg_dlf_1d_export(int k, int n, int64_t* rowptr, int32_t* col, double* val) {
+    API_BEGIN
+    NEED(rowptr);
+    NEED(col);
+    NEED(val);
+    CSR A = dlf_csr(k, n);
+    std::memcpy(rowptr, A.rowptr.data(), sizeof(int64_t) * A.rowptr.size());
+    std::memcpy(col, A.col.data(), sizeof(int32_t) * A.col.size());
+    std::memcpy(val, A.val.data(), sizeof(double) * A.val.size());
+    API_END
+}
+
+int sgdg_op_create(int D, int k, int n, int scheme, sgdg_op** out) {
+    API_BEGIN
+    NEED(out);
+    *out = nullptr;
+    if (n < 2) throw Error(SGDG_EINVAL, "n must be >= 2");
+    auto op = std::make_unique<sgdg_op>();
+    op->ix = make_index(D, k, n, scheme);
+    op->dlf = dlf1d(k, n);
+    op->dd.resize(D);
+    *out = op.release();
+    API_END
+}
+
+int sgdg_op_destroy(sgdg_op* op) {
+    API_BEGIN
+    delete op;
+    API_END
+}
+
+int sgdg_op_size(const sgdg_op* op, int64_t* N) {
+    API_BEGIN
+    NEED(op);
+    NEED(N);
+    *N = op->ix.N;
+    API_END
+}
+
+int sgdg_op_nnz(sgdg_op* op, int which, int64_t* nnz) {
+    API_BEGIN
+    NEED(op);
+    NEED(nnz);
+    *nnz = op->get(which).nnz();
+    API_END
+}
+
+int sgdg_op_export_csr(sgdg_op* op, int which, int64_t* rowptr, int32_t* col, double* val) {
+    API_BEGIN
+    NEED(op);
+    NEED(rowptr);
+    NEED(col);
+    NEED(val);
+    const CSR& A = op->get(which);
+    std::memcpy(rowptr, A.rowptr.data(), sizeof(int64_t) * A.rowptr.size());
+    std::memcpy(col, A.col.data(), sizeof(int32_t) * A.col.size());
+    std::memcpy(val, A.val.data(), sizeof(double) * A.val.size());
+    API_END
+}
+
+static void apply_device_impl(sgdg_op* op, int which, int method, const double* x, double* y, cudaStream_t st) {
+    if (method == SGDG_METHOD_PLAIN) {
+        const DevCSR& A = op->device(which);
+        CK(launch_csr_spmv(A, x, y, st));
+        return;
+    }
+    if (method != SGDG_METHOD_MATFREE) throw Error(SGDG_EINVAL, "method must be PLAIN (0) or MATFREE (1)");
+    if (!(which == SGDG_OP_LAPLACIAN || (which >= 1 && which <= op->ix.D)))
+        throw Error(SGDG_EUNSUPPORTED, "matrix-free apply supports which = 1..D or 0 (laplacian)");
+    auto it = op->mf_apply.find(which);
+    if (it == op->mf_apply.end()) {
+        auto eng = std::make_unique<MFEngine>(st);
+        SolveSpec sp{};
+        sp.kind = which == SGDG_OP_LAPLACIAN ? MF_KIND_WAVE : MF_KIND_ADVECT;
+        sp.D = op->ix.D;
+        sp.k = op->ix.k;
+        sp.n = op->ix.n;
+        sp.scheme = op->ix.scheme;
+        sp.dt = 0.0;
+        sp.apply_dim = which >= 1 ? which - 1 : -1;
+        eng->add(sp, nullptr);
+        it = op->mf_apply.emplace(which, std::move(eng)).first;
+    }
+    it->second->set_stream(st);
+    it->second->load_input_device(0, x);
+    it->second->run_apply(y);
+}
+
+int sgdg_apply(sgdg_op* op, int which, int method, const double* x, double* y) {
+    API_BEGIN
+    NEED(op);
+    NEED(x);
+    NEED(y);
+    cudaStream_t st = op_stream(op);
+    const int64_t len = which == SGDG_OP_WAVE_RHS ? 2 * op->ix.N : op->ix.N;
+    op->get(which);
+    DevBuf dx(sizeof(double) * len), dy(sizeof(double) * len);
+    CK(cudaMemcpyAsync(dx.p, x, sizeof(double) * len, cudaMemcpyHostToDevice, st));
+    apply_device_impl(op, which, method, dx.as<double>(), dy.as<double>(), st);
+    CK(cudaMemcpyAsync(y, dy.p, sizeof(double) * len, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    API_END
+}
+
+int sgdg_apply_device(sgdg_op* op, int which, int method, const double* x_dev, double* y_dev, void* stream) {
+    API_BEGIN
+    NEED(op);
+    NEED(x_dev);
+    NEED(y_dev);
+    require_gpu();
+    apply_device_impl(op, which, method, x_dev, y_dev, (cudaStream_t)stream);
+    API_END
+}
+
+static std::vector<int64_t> out_steps(int64_t nsteps, int nout) {
+    std::vector<int64_t> s(nout);
+    for (int i = 0; i < nout; i++) s[i] = (int64_t)((__int128)nsteps * i / (nout - 1));
+    return s;
+}
+
+static void plain_evolve(sgdg_op* op, int which_or_adv, const CSR* Aadv, const double* y0, int64_t len, double t0,
+                         double t1, int64_t nsteps, int nout, double* times, double* states) {
+    cudaStream_t st = op_stream(op);
+    std::unique_ptr<DeviceCSR> own;
+    const DevCSR* A;
+    if (Aadv) {
+        own = to_device(*Aadv, st);
+        A = &own->d;
+    } else {
+        A = &op->device(which_or_adv);
+    }
+    DevBuf y(sizeof(double) * len), acc(sizeof(double) * len), u0(sizeof(double) * len), u1(sizeof(double) * len);
+    CK(cudaMemcpyAsync(y.p, y0, sizeof(double) * len, cudaMemcpyHostToDevice, st));
+    const double dt = (t1 - t0) / double(nsteps);
+    // one RK4 step as a graph
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = launch_csr_rk4(*A, y.as<double>(), y.as<double>(), acc.as<double>(), u0.as<double>(), dt, 1, st);
+    if (e == cudaSuccess)
+        e = launch_csr_rk4(*A, u0.as<double>(), y.as<double>(), acc.as<double>(), u1.as<double>(), dt, 2, st);
+    if (e == cudaSuccess)
+        e = launch_csr_rk4(*A, u1.as<double>(), y.as<double>(), acc.as<double>(), u0.as<double>(), dt, 3, st);
+    if (e == cudaSuccess)
+        e = launch_csr_rk4(*A, u0.as<double>(), y.as<double>(), acc.as<double>(), u1.as<double>(), dt, 4, st);
+    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        throw Error(SGDG_ECUDA, std::string("capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) throw Error(SGDG_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e3));
+    auto steps = out_steps(nsteps, nout);
+    int64_t done = 0;
+    cudaError_t err = cudaSuccess;
+    for (int i = 0; i < nout && err == cudaSuccess; i++) {
+        for (; done < steps[i] && err == cudaSuccess; done++) err = cudaGraphLaunch(ge, st);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(states + (size_t)i * len, y.p, sizeof(double) * len, cudaMemcpyDeviceToHost, st);
+        if (times) times[i] = t0 + (t1 - t0) * double(steps[i]) / double(nsteps);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    cudaGraphExecDestroy(ge);
+    if (err != cudaSuccess) throw Error(SGDG_ECUDA, std::string("evolve: ") + cudaGetErrorString(err));
+}
+
+static void mf_evolve(sgdg_op* op, int kind, const double* a, const double* y0, int64_t len, double t0, double t1,
+                      int64_t nsteps, int nout, double* times, double* states) {
+    cudaStream_t st = op_stream(op);
+    MFEngine eng(st);
+    SolveSpec sp{};
+    sp.kind = kind;
+    sp.D = op->ix.D;
+    sp.k = op->ix.k;
+    sp.n = op->ix.n;
+    sp.scheme = op->ix.scheme;
+    for (int d = 0; d < sp.D; d++) sp.a[d] = a ? a[d] : 0.0;
+    sp.dt = (t1 - t0) / double(nsteps);
+    sp.apply_dim = -1;
+    int id = eng.add(sp, y0);
+    auto steps = out_steps(nsteps, nout);
+    int64_t done = 0;
+    for (int i = 0; i < nout; i++) {
+        eng.step(steps[i] - done);
+        done = steps[i];
+        eng.get_state(id, states + (size_t)i * len);
+        if (times) times[i] = t0 + (t1 - t0) * double(steps[i]) / double(nsteps);
+    }
+}
+
+static void check_evolve_args(int64_t nsteps, int nout, double t0, double t1) {
+    if (nsteps < 1) throw Error(SGDG_EINVAL, "nsteps must be >= 1");
+    if (nout < 2) throw Error(SGDG_EINVAL, "nout must be >= 2");
+    if (!(std::isfinite(t0) && std::isfinite(t1)) || t1 == t0) throw Error(SGDG_EINVAL, "need finite t0 != t1");
+}
+
+int sgdg_wave_evolve(sgdg_op* op, const double* f0, const double* v0, double t0, double t1, int64_t nsteps, int nout,
+                     int method, double* times, double* states) {
+    API_BEGIN
+    NEED(op);
+    NEED(f0);
+    NEED(v0);
+    NEED(states);
+    check_evolve_args(nsteps, nout, t0, t1);
+    const int64_t N = op->ix.N;
+    std::vector<double> y0(2 * N);
+    std::memcpy(y0.data(), f0, sizeof(double) * N);
+    std::memcpy(y0.data() + N, v0, sizeof(double) * N);
+    if (method == SGDG_METHOD_PLAIN)
+        plain_evolve(op, SGDG_OP_WAVE_RHS, nullptr, y0.data(), 2 * N, t0, t1, nsteps, nout, times, states);
+    else if (method == SGDG_METHOD_MATFREE)
+        mf_evolve(op, MF_KIND_WAVE, nullptr, y0.data(), 2 * N, t0, t1, nsteps, nout, times, states);
+    else
+        throw Error(SGDG_EINVAL, "method must be PLAIN (0) or MATFREE (1)");
+    API_END
+}
+
+int sgdg_advect_evolve(sgdg_op* op, const double* a, const double* f0, double t0, double t1, int64_t nsteps, int nout,
+                       int method, double* times, double* states) {
+    API_BEGIN
+    NEED(op);
+    NEED(a);
+    NEED(f0);
+    NEED(states);
+    check_evolve_args(nsteps, nout, t0, t1);
+    const int64_t N = op->ix.N;
+    if (method == SGDG_METHOD_PLAIN) {
+        std::vector<const CSR*> v;
+        std::vector<double> s;
+        for (int d = 1; d <= op->ix.D; d++) {
+            v.push_back(&op->get(d));
+            s.push_back(-a[d - 1]);
+        }
+        CSR A = add_scaled(v, s);
+        plain_evolve(op, 0, &A, f0, N, t0, t1, nsteps, nout, times, states);
+    } else if (method == SGDG_METHOD_MATFREE) {
+        mf_evolve(op, MF_KIND_ADVECT, a, f0, N, t0, t1, nsteps, nout, times, states);
+    } else {
+        throw Error(SGDG_EINVAL, "method must be PLAIN (0) or MATFREE (1)");
+    }
+    API_END
+}
+
+// ------------------------------------------------------------ batches ----
+int sgdg_batch_create(sgdg_batch** out) {
+    API_BEGIN
+    NEED(out);
+    require_gpu();
+    auto b = std::make_unique<sgdg_batch>();
+    CK(cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking));
+    b->eng.set_stream(b->own);
+    *out = b.release();
+    API_END
+}
+
+int sgdg_batch_destroy(sgdg_batch* b) {
+    API_BEGIN
+    if (b) cudaStreamSynchronize(b->eng.stream());
+    delete b;
+    API_END
+}
+
+int sgdg_batch_add(sgdg_batch* b, int kind, int D, int k, int n, int scheme, const double* a, double dt,
+                   const double* y0, int* id) {
+    API_BEGIN
+    NEED(b);
+    NEED(y0);
+    NEED(id);
+    if (kind != SGDG_KIND_ADVECT && kind != SGDG_KIND_WAVE) throw Error(SGDG_EINVAL, "kind must be ADVECT or WAVE");
+    if (kind == SGDG_KIND_ADVECT) NEED(a);
+    if (n < 2) throw Error(SGDG_EINVAL, "n must be >= 2");
+    if (!std::isfinite(dt)) throw Error(SGDG_EINVAL, "dt must be finite");
+    SolveSpec sp{};
+    sp.kind = kind == SGDG_KIND_WAVE ? MF_KIND_WAVE : MF_KIND_ADVECT;
+    sp.D = D;
+    sp.k = k;
+    sp.n = n;
+    sp.scheme = scheme;
+    for (int d = 0; d < D && d < 8; d++) sp.a[d] = a ? a[d] : 0.0;
+    sp.dt = dt;
+    sp.apply_dim = -1;
+    *id = b->eng.add(sp, y0);
+    API_END
+}
+
+int sgdg_batch_remove(sgdg_batch* b, int id) {
+    API_BEGIN
+    NEED(b);
+    b->eng.remove(id);
+    API_END
+}
+
+int sgdg_batch_set_stream(sgdg_batch* b, void* stream) {
+    API_BEGIN
+    NEED(b);
+    b->eng.set_stream(stream ? (cudaStream_t)stream : b->own);
+    API_END
+}
+
+int sgdg_batch_step(sgdg_batch* b, int64_t nsteps) {
+    API_BEGIN
+    NEED(b);
+    if (nsteps < 0) throw Error(SGDG_EINVAL, "nsteps must be >= 0");
+    b->eng.step(nsteps);
+    API_END
+}
+
+int sgdg_batch_get_state(sgdg_batch* b, int id, double* y) {
+    API_BEGIN
+    NEED(b);
+    NEED(y);
+    b->eng.get_state(id, y);
+    API_END
+}
+
+int sgdg_batch_state_size(sgdg_batch* b, int id, int64_t* len) {
+    API_BEGIN
+    NEED(b);
+    NEED(len);
+    *len = b->eng.at(id).Ns;
+    API_END
+}
+
+int sgdg_batch_step_info(sgdg_batch* b, int64_t* launches, double* dofs) {
+    API_BEGIN
+    NEED(b);
+    if (launches) *launches = b->eng.launches_per_step();
+    if (dofs) *dofs = b->eng.dof_updates_per_step();
+    API_END
+}
+
+int sgdg_set_hbm_budget(int64_t bytes) {
+    API_BEGIN
+    if (bytes < 0) throw Error(SGDG_EINVAL, "budget must be >= 0");
+    g_budget = bytes;
+    API_END
+}
+
+int sgdg_hbm_in_use(int64_t* bytes) {
+    API_BEGIN
+    NEED(bytes);
+    *bytes = g_in_use.load();
+    API_END
+}
+
+int sgdg_sync(void) {
+    API_BEGIN
+    require_gpu();
+    CK(cudaDeviceSynchronize());
+    API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+// sgdg_core.h -- internal host-side structures of libsgdg (not part of the C ABI).
+//
+// Naming follows GalerkinSparseGrids.jl: levels are 1-based like the reference's
+// CartesianIndex levels (level L means hierarchical level L-1), cells and modes
+// are 1-based in the public index map and 0-based inside the library.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace sgdg {
+
+constexpr int kKMax = 10;  // K_max, src/1d_dg_functions.jl:198
+constexpr int kDMax = 8;   // largest dimension the library indexes
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// ---------------------------------------------------------------- basis ----
+// Hierarchical multiwavelet basis on [-1,1] (src/dg_basis.jl:185-190) and the
+// normalised Legendre polynomials (src/dg_basis.jl:88-94).  A basis function
+// is stored as 2k coefficients: x^i for i<k and sgn(x) x^i for i>=k.
+struct Basis1D {
+    int k = 0;
+    std::vector<double> dg;   // dg[mode*2k + coef]
+    std::vector<double> leg;  // leg[m*(kKMax+1)... ] normalised Legendre, m=0..kKMax, monomial coeffs
+};
+const Basis1D& basis(int k);
+
+// Polynomial piece (monomial coefficients in the local variable y) of one
+// hierarchical function; evaluation helpers return value / derivative in x.
+struct HierFn {
+    int level;   // 0-based hierarchical level (0 = Legendre level)
+    int cell;    // 1-based
+    int mode;    // 1-based
+    double x0, xm, x1;          // support and midpoint (xm unused at level 0)
+    double scale, dydx, shift;  // v(x) = scale * p(dydx*x - shift)
+    double left[kKMax], right[kKMax];  // p on y<0 (or the whole piece at level 0) / y>0
+    int k;
+};
+HierFn make_hier_fn(int k, int level, int cell, int mode);
+// One-sided limits at x (side=+1 from the right, -1 from the left), periodic on [0,1).
+double hier_value(const HierFn& f, double x, int side);
+double hier_deriv(const HierFn& f, double x, int side);
+
+// ----------------------------------------------------------- 1D operator ----
+// Hierarchical periodic DG derivative with central flux, the operator that
+// src/1d_derivative.jl:113-117 builds as hier2pos' * A * hier2pos.  Block
+// sparse: one dense k x k block for every pair of (level, cell) blocks whose
+// closed supports meet periodically.  Blocks are numbered in the reference's
+// 1D vector order (levels 1..n+1, cells, modes).
+struct DLF1D {
+    int k = 0, n = 0;
+    int nblocks = 0;                 // 2^n
+    std::vector<int> blk_level;      // 1-based level of each block
+    std::vector<int> blk_cell;       // 1-based cell
+    std::vector<int32_t> rowptr;     // block-CSR by row block, nblocks+1
+    std::vector<int32_t> colblk;     // column block per stored block (sorted per row)
+    std::vector<double> val;         // k*k per stored block, [i][j] = D[rb*k+i][cb*k+j]
+};
+std::shared_ptr<const DLF1D> dlf1d(int k, int n);
+
+// ------------------------------------------------------------ index map ----
+// Sparse-grid coefficient layout of src/dg_vmethods.jl:246-286: level tuples
+// in Julia CartesianIndices order (dimension 1 fastest), then cells, then modes.
+struct SparseIndex {
+    int D = 0, k = 0, n = 0, scheme = 0;
+    int64_t N = 0, kD = 1;
+    int nlev = 0;
+    std::vector<int> levels;        // nlev x D, 1-based
+    std::vector<int64_t> lev_off;   // nlev
+    std::vector<int64_t> lev_cells; // nlev (product of cells)
+    std::vector<int32_t> code2lev;  // (n+1)^D -> level block id or -1
+    int64_t code(const int* L) const;
+    int lookup_level(const int* L) const { return code2lev[code(L)]; }
+    bool cut(const int* L) const;
+};
+SparseIndex make_index(int D, int k, int n, int scheme);
+inline int64_t ncells(int L) { return int64_t(1) << (L > 2 ? L - 2 : 0); }
+inline int log2cells(int L) { return L > 2 ? L - 2 : 0; }
+
+// ------------------------------------------------------------------ CSR ----
+struct CSR {
+    int64_t m = 0, n = 0;
+    std::vector<int64_t> rowptr;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+    int64_t nnz() const { return rowptr.empty() ? 0 : rowptr.back(); }
+};
+CSR assemble_dd(const SparseIndex& ix, const DLF1D& op, int d);              // D_matrix(D,d,k,n)
+CSR spgemm_sum(const std::vector<const CSR*>& A);                  // sum_i A_i * A_i
+CSR add_scaled(const std::vector<const CSR*>& A, const std::vector<double>& s);
+CSR wave_rhs(const CSR& lap);                                                // wave_data
+
+// ------------------------------------------------------ pencil schedule ----
+// A pencil for dimension d fixes the levels of every other dimension; its
+// elements are whole level blocks (L_-d, l) for l = 1..Lmax and form an
+// m x R matrix: rows = 1D prefix of length k*2^(Lmax-1), columns = the other
+// dimensions' cells and modes.
+struct Pencil {
+    int d;                 // 0-based dimension
+    int lmax;              // 1-based max level along d
+    int64_t R;             // columns
+    int lp;                // log2 of prod_{q<d} cells_q
+    std::vector<int64_t> blockoff;  // offset of level block (L_-d, l), l = 1..lmax
+};
+std::vector<Pencil> make_pencils(const SparseIndex& ix, int d);
+
+void set_error(const std::string& msg);
+}  // namespace sgdg

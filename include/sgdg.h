@@ -1,0 +1,141 @@
+/*
+ * sgdg.h -- C ABI of libsgdg: the sparse-grid DG derivative operator of
+ * GalerkinSparseGrids.jl applied inside explicit Runge-Kutta time stepping on
+ * one NVIDIA GB300 (sm_103a).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (SGDG_OK = 0); the message of
+ *    the last failure on the calling thread is read with sgdg_last_error.
+ *    Nothing throws or aborts across this boundary.
+ *  - Coefficient vectors use the reference's layout exactly (levels in
+ *    column-major CartesianIndices order, then cells, then modes;
+ *    src/dg_vmethods.jl:246-286), so a Julia Vector{Float64} from vcoeffs_DG
+ *    passes through unchanged.  Arrays are caller-owned; pointers named *_dev
+ *    are device pointers, all others are host memory.
+ *  - Indices in exported CSR arrays are 0-based; level/cell/mode in
+ *    sgdg_index_map are 1-based like the reference.
+ *  - Handles are not safe for concurrent use from several threads; distinct
+ *    handles are independent.  Compute calls need a CUDA GPU and fail with
+ *    SGDG_ENOGPU otherwise (there is no CPU fallback).
+ */
+#ifndef SGDG_H
+#define SGDG_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    SGDG_OK = 0,
+    SGDG_EINVAL = 1,          /* bad argument (the reference throws ArgumentError/DomainError) */
+    SGDG_ENOMEM_BUDGET = 2,   /* device allocation refused by the HBM budget or by the device */
+    SGDG_ETIMEOUT = 3,        /* a bounded device wait gave up                                 */
+    SGDG_ECUDA = 4,           /* CUDA runtime error                                            */
+    SGDG_ECANCELLED = 5,      /* the request was cancelled                                     */
+    SGDG_ENOGPU = 6,          /* no usable CUDA device                                         */
+    SGDG_EUNSUPPORTED = 7     /* valid input outside what this build implements                */
+};
+
+enum { SGDG_SCHEME_SPARSE = 0, SGDG_SCHEME_FULL = 1 };
+
+/* Plain form: assembled FP64 CSR SpMV + FP64 RK4 update (the drop-in).
+ * Matrix-free form: FP32 pencil apply of the 1D blocks, FP64 RK4 state.  */
+enum { SGDG_METHOD_PLAIN = 0, SGDG_METHOD_MATFREE = 1 };
+
+/* Operator selector "which": 1..D = D_matrix(D,d,k,n); 0 = laplacian_matrix;
+ * -1 = the wave right-hand side [[0, I], [L, 0]] of wave_data.              */
+enum { SGDG_OP_LAPLACIAN = 0, SGDG_OP_WAVE_RHS = -1 };
+
+/* Problem kinds of batched / served solves. */
+enum { SGDG_KIND_ADVECT = 0, SGDG_KIND_WAVE = 1 };
+
+typedef struct sgdg_op sgdg_op;
+typedef struct sgdg_batch sgdg_batch;
+
+/* Library version string and the last error message of this thread. */
+int sgdg_version(char *buf, size_t len);
+int sgdg_last_error(char *buf, size_t len);
+
+/* ---- index map ---------------------------------------------------------- */
+/* get_size (src/dg_vmethods.jl:179-189). */
+int sgdg_get_size(int D, int k, int n, int scheme, int64_t *N);
+/* V2Dref (src/dg_vmethods.jl:267-286): N x D arrays (row-major, entry [i*D+q])
+ * of 1-based level, cell and mode of every coefficient. */
+int sgdg_index_map(int D, int k, int n, int scheme, int32_t *level, int32_t *cell, int32_t *mode);
+/* dg_coeffs[k] (src/1d_dg_functions.jl:243-253): 2k x k, column-major
+ * (out[mode*2k + i]; i < k: x^i, i >= k: sgn(x) x^(i-k)). */
+int sgdg_dg_coeffs(int k, double *out);
+
+/* ---- 1D operator -------------------------------------------------------- */
+/* periodic_DLF_matrix(k, n) (src/1d_derivative.jl:113-117,136-148), CSR. */
+int sgdg_dlf_1d_nnz(int k, int n, int64_t *nnz);
+int sgdg_dlf_1d_export(int k, int n, int64_t *rowptr, int32_t *col, double *val);
+
+/* ---- operators ---------------------------------------------------------- */
+/* Operator handle for (D, k, n, scheme); replaces the setup of
+ * D_matrix / grad_matrix / laplacian_matrix (src/multidim_derivative.jl:209-227).
+ * Requires n >= 2 and 1 <= k <= 10. */
+int sgdg_op_create(int D, int k, int n, int scheme, sgdg_op **out);
+int sgdg_op_destroy(sgdg_op *op);
+int sgdg_op_size(const sgdg_op *op, int64_t *N);
+/* Stored entries of the assembled operator `which` (numerical zeros counted). */
+int sgdg_op_nnz(sgdg_op *op, int which, int64_t *nnz);
+/* The assembled operator as CSR (rowptr: rows+1 entries; columns sorted). */
+int sgdg_op_export_csr(sgdg_op *op, int which, int64_t *rowptr, int32_t *col, double *val);
+
+/* y = A x for operator `which` -- the RHS closure (t,x)->*(RHS,x) of
+ * src/pdes.jl:63.  Host buffers (length N, or 2N for SGDG_OP_WAVE_RHS).
+ * SGDG_METHOD_MATFREE supports which = 1..D and SGDG_OP_LAPLACIAN. */
+int sgdg_apply(sgdg_op *op, int which, int method, const double *x, double *y);
+/* Same with device pointers on a caller stream (cudaStream_t, may be NULL). */
+int sgdg_apply_device(sgdg_op *op, int which, int method, const double *x_dev, double *y_dev, void *stream);
+
+/* ---- evolvers ----------------------------------------------------------- */
+/* wave_evolve (src/pdes.jl:54-70) with classical RK4 and nsteps fixed steps on
+ * [t0, t1]: u_tt = laplacian(u), state [f; v].  Writes nout >= 2 equally
+ * spaced states (times[nout], states[nout * 2N], the first is the initial
+ * state), like ODE.jl's (times, states) at the requested output points. */
+int sgdg_wave_evolve(sgdg_op *op, const double *f0, const double *v0, double t0, double t1, int64_t nsteps,
+                     int nout, int method, double *times, double *states);
+/* Linear advection f_t = -sum_d a_d D_d f (velocity a[D]), composed from
+ * grad_matrix the way wave_evolve composes laplacian_matrix. */
+int sgdg_advect_evolve(sgdg_op *op, const double *a, const double *f0, double t0, double t1, int64_t nsteps,
+                       int nout, int method, double *times, double *states);
+
+/* ---- batches of independent solves (matrix-free form) ------------------- */
+/* Many solves of uneven D, k, n advance together: each RK stage is one
+ * launch per dimension over the tiles of every solve, replayed from a CUDA
+ * graph.  State stays on the device between calls. */
+int sgdg_batch_create(sgdg_batch **out);
+int sgdg_batch_destroy(sgdg_batch *b);
+/* Adds a solve; y0 has N (advection) or 2N (wave: [f; v]) coefficients;
+ * a[D] is the advection velocity (ignored for the wave).  Returns its id. */
+int sgdg_batch_add(sgdg_batch *b, int kind, int D, int k, int n, int scheme, const double *a, double dt,
+                   const double *y0, int *id);
+/* Removes a solve and frees its device state (ids of others are unchanged). */
+int sgdg_batch_remove(sgdg_batch *b, int id);
+/* Use a caller stream (cudaStream_t) for all work of this batch. */
+int sgdg_batch_set_stream(sgdg_batch *b, void *stream);
+/* Advances every solve in the batch by nsteps RK4 steps (asynchronous). */
+int sgdg_batch_step(sgdg_batch *b, int64_t nsteps);
+/* Copies solve `id`'s state to the host (synchronises the batch stream). */
+int sgdg_batch_get_state(sgdg_batch *b, int id, double *y);
+/* Number of stored state coefficients of solve `id` (N or 2N). */
+int sgdg_batch_state_size(sgdg_batch *b, int id, int64_t *len);
+/* Launch statistics of one batch step: kernel launches and algorithmic bytes
+ * (32 B per state coefficient per RK stage). */
+int sgdg_batch_step_info(sgdg_batch *b, int64_t *launches_per_step, double *dof_updates_per_step);
+
+/* ---- resources ---------------------------------------------------------- */
+/* Upper bound on device bytes the library may hold (0 = no limit). */
+int sgdg_set_hbm_budget(int64_t bytes);
+int sgdg_hbm_in_use(int64_t *bytes);
+/* Blocks until all library work on the device has finished. */
+int sgdg_sync(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGDG_H */

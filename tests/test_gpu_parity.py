@@ -1,0 +1,185 @@
+"""GPU parity: libsgdg's kernels through the C ABI against the FP64 oracle.
+
+Tolerances: plain FP64 form 1e-10 relative L2 (roundoff of a different
+summation order and of the 1D entries, ~1e-13 apart); matrix-free FP32 form
+1e-6 relative L2 for evolved states (the stated error budget) and 5e-7 for a
+single operator application."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RNG = np.random.default_rng(20261203)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def fourier_ic(sg, D, k, n, nmodes, seed, amax=3):
+    rng = np.random.default_rng(seed)
+    modes = []
+    for _ in range(nmodes):
+        a = tuple(int(v) for v in rng.integers(1, amax + 1, size=D))
+        modes.append((a, float(rng.uniform(-1, 1)), "sin" if rng.random() < 0.5 else "cos", 0.0))
+    return sg.fourier_coeffs(D, k, n, modes)
+
+
+@pytest.mark.parametrize("D,k,n", [(2, 3, 5), (3, 2, 4), (3, 3, 4), (2, 1, 4), (1, 4, 5)])
+def test_apply_plain_matches_oracle(sgdg, O, D, k, n):
+    op = sgdg.SparseGridOperator(D, k, n)
+    x = RNG.standard_normal(op.N)
+    for d in range(1, D + 1):
+        y = op.apply(x, d, "plain")
+        ref = O.spmv_csc(O.D_matrix_raw(D, d, k, n), x)
+        assert rel(y, ref) < 1e-10
+    y = op.apply(x, 0, "plain")
+    assert rel(y, O.spmv_csc(O.laplacian_matrix_raw(D, k, n), x)) < 1e-10
+    x2 = RNG.standard_normal(2 * op.N)
+    y2 = op.apply(x2, -1, "plain")
+    assert rel(y2, O.spmv_csc(O.wave_rhs_raw(D, k, n), x2)) < 1e-10
+
+
+@pytest.mark.parametrize("D,k,n", [(2, 3, 5), (3, 2, 4), (3, 3, 4), (2, 4, 4), (2, 1, 4), (4, 2, 4), (1, 5, 5)])
+def test_apply_matfree_matches_oracle(sgdg, O, D, k, n):
+    op = sgdg.SparseGridOperator(D, k, n)
+    x = fourier_ic(sgdg, D, k, n, 3, seed=D * 10 + k) + 1e-3 * RNG.standard_normal(op.N)
+    for d in range(1, D + 1):
+        y = op.apply(x, d, "matfree")
+        ref = O.spmv_csc(O.D_matrix_raw(D, d, k, n), x)
+        assert rel(y, ref) < 5e-7
+    y = op.apply(x, 0, "matfree")
+    assert rel(y, O.spmv_csc(O.laplacian_matrix_raw(D, k, n), x)) < 1e-6
+
+
+def test_full_scheme_apply(sgdg, O):
+    D, k, n = 2, 2, 3
+    op = sgdg.SparseGridOperator(D, k, n, "full")
+    x = RNG.standard_normal(op.N)
+    for d in (1, 2):
+        ref = O.spmv_csc(O._Mat(O.lib().or_dmatrix(D, d, k, n, 1)), x)
+        assert rel(op.apply(x, d, "plain"), ref) < 1e-10
+        assert rel(op.apply(x, d, "matfree"), ref) < 5e-7
+
+
+def _cfg1(sgdg):
+    D, k, n = 2, 3, 5
+    f0 = fourier_ic(sgdg, D, k, n, 4, seed=1)
+    a = np.random.default_rng(2).uniform(-1, 1, size=D)
+    return D, k, n, f0, a
+
+
+def test_cfg1_advection_plain_and_matfree(sgdg, O):
+    # 2D, sparse k=3 n=5, 4 seeded Fourier modes, RK4 dt=1e-3 to t=1
+    D, k, n, f0, a = _cfg1(sgdg)
+    ref = O.CSR(O.advection_matrix_raw(D, k, n, a)).rk4(f0, 1e-3, 1000, nthreads=8)
+    _, st = sgdg.advect_evolve(D, k, n, a, f0, 0.0, 1.0, dt=1e-3, method="plain")
+    assert rel(st[-1], ref) < 1e-10
+    _, st = sgdg.advect_evolve(D, k, n, a, f0, 0.0, 1.0, dt=1e-3, method="matfree")
+    assert rel(st[-1], ref) < 1e-6
+    assert np.max(np.abs(st[-1] - ref)) < 1e-6 * np.max(np.abs(ref)) * 10
+
+
+def test_cfg1_wave_plain_and_matfree(sgdg, O):
+    D, k, n, f0, _ = _cfg1(sgdg)
+    v0 = fourier_ic(sgdg, D, k, n, 4, seed=3)
+    ref = O.CSR(O.wave_rhs_raw(D, k, n)).rk4(np.concatenate([f0, v0]), 1e-3, 1000, nthreads=8)
+    times, st = sgdg.wave_evolve(D, k, n, f0, v0, 0.0, 1.0, dt=1e-3, nout=3, method="plain")
+    assert np.allclose(times, [0.0, 0.5, 1.0])
+    assert np.array_equal(st[0], np.concatenate([f0, v0]))
+    assert rel(st[-1], ref) < 1e-10
+    _, st = sgdg.wave_evolve(D, k, n, f0, v0, 0.0, 1.0, dt=1e-3, method="matfree")
+    assert rel(st[-1], ref) < 1e-6
+
+
+def test_wave_energy_known_answer_gpu(sgdg):
+    # test/solvers.jl:51-75 on the GPU: sqrt(E) = sqrt(2) pi +- 1e-4, decreasing
+    D, k, n = 2, 3, 5
+    s = sgdg.vcoeffs_1d(k, n, lambda x: np.sin(2 * np.pi * x))
+    f0 = sgdg.tensor_construct(D, k, n, [s, s])
+    v0 = np.zeros_like(f0)
+    for method, drift in (("plain", 1e-8), ("matfree", 1e-5)):
+        soln = sgdg.wave_evolve(D, k, n, f0, v0, 0.0, 1.0, dt=1e-3, nout=6, method=method)
+        _, E = sgdg.energy_func(D, k, n, soln)
+        assert abs(E[0] - E[-1]) < drift
+        if method == "plain":
+            assert E[0] - E[-1] > 0
+        assert np.all(np.abs(np.sqrt(E) - np.sqrt(2) * np.pi) < 1e-4)
+
+
+@pytest.fixture(scope="module")
+def cfg2(sgdg, O):
+    """3D wave, sparse k=3 n=7, seeded 6-mode Fourier IC, RK4 to t=1 (dt=2.5e-3:
+    spectral radius 1034, rho*dt = 2.58 < 2.8)."""
+    D, k, n = 3, 3, 7
+    f0 = fourier_ic(sgdg, D, k, n, 6, seed=11)
+    v0 = fourier_ic(sgdg, D, k, n, 6, seed=12)
+    y0 = np.concatenate([f0, v0])
+    ref = O.CSR(O.wave_rhs_raw(D, k, n)).rk4(y0, 2.5e-3, 400, nthreads=O.max_threads())
+    return D, k, n, f0, v0, ref
+
+
+def test_cfg2_wave3d_plain(sgdg, cfg2):
+    D, k, n, f0, v0, ref = cfg2
+    _, st = sgdg.wave_evolve(D, k, n, f0, v0, 0.0, 1.0, dt=2.5e-3, method="plain")
+    assert rel(st[-1], ref) < 1e-10
+
+
+def test_cfg2_wave3d_matfree_error_budget(sgdg, cfg2):
+    D, k, n, f0, v0, ref = cfg2
+    _, st = sgdg.wave_evolve(D, k, n, f0, v0, 0.0, 1.0, dt=2.5e-3, method="matfree")
+    e2 = rel(st[-1], ref)
+    einf = float(np.max(np.abs(st[-1] - ref)) / np.max(np.abs(ref)))
+    print("cfg2 matfree: rel L2 %.3e  rel Linf %.3e" % (e2, einf))
+    assert e2 < 1e-6
+
+
+def test_batch_mixed_equals_alone_and_oracle(sgdg, O):
+    specs = [("advect", 2, 2, 4), ("advect", 3, 3, 4), ("wave", 2, 3, 5), ("advect", 2, 4, 5), ("advect", 3, 2, 5),
+             ("wave", 3, 2, 4)]
+    rng = np.random.default_rng(7)
+    dt, steps = 1e-3, 100
+    b = sgdg.Batch()
+    ids, ys, avs = [], [], []
+    for i, (kind, D, k, n) in enumerate(specs):
+        f0 = fourier_ic(sgdg, D, k, n, 3, seed=100 + i)
+        a = rng.uniform(-1, 1, size=D)
+        y0 = np.concatenate([f0, fourier_ic(sgdg, D, k, n, 3, seed=200 + i)]) if kind == "wave" else f0
+        ids.append(b.add(kind, D, k, n, y0, dt, a=a if kind == "advect" else None))
+        ys.append(y0)
+        avs.append(a)
+    b.step(steps)
+    for i, (kind, D, k, n) in enumerate(specs):
+        got = b.state(ids[i])
+        alone = sgdg.Batch()
+        j = alone.add(kind, D, k, n, ys[i], dt, a=avs[i] if kind == "advect" else None)
+        alone.step(steps)
+        assert np.array_equal(got, alone.state(j)), "solve %d differs alone vs mixed" % i
+        if kind == "advect":
+            ref = O.CSR(O.advection_matrix_raw(D, k, n, avs[i])).rk4(ys[i], dt, steps, nthreads=8)
+        else:
+            ref = O.CSR(O.wave_rhs_raw(D, k, n)).rk4(ys[i], dt, steps, nthreads=8)
+        assert rel(got, ref) < 1e-6
+
+
+def test_batch_remove_and_budget(sgdg):
+    b = sgdg.Batch()
+    D, k, n = 2, 2, 4
+    y0 = fourier_ic(sgdg, D, k, n, 2, seed=5)
+    i0 = b.add("advect", D, k, n, y0, 1e-3, a=[0.5, -0.25])
+    i1 = b.add("advect", D, k, n, y0, 1e-3, a=[0.5, -0.25])
+    b.step(10)
+    s0 = b.state(i0)
+    b.remove(i0)
+    b.step(0)
+    with pytest.raises(sgdg.SGDGError):
+        b.state(i0)
+    assert np.array_equal(b.state(i1), s0)
+    used = sgdg.hbm_in_use()
+    sgdg.set_hbm_budget(used + 1024)
+    try:
+        with pytest.raises(sgdg.SGDGError) as e:
+            b.add("advect", 3, 3, 6, np.zeros(sgdg.get_size(3, 3, 6)), 1e-3, a=[1.0, 0.0, 0.0])
+        assert e.value.code == 2
+    finally:
+        sgdg.set_hbm_budget(0)
