@@ -12,6 +12,7 @@ Host-side helpers here (coefficient projection, index maps, sparse exports)
 are set-up and I/O around the hot path, like the reference's own set-up code.
 """
 import ctypes
+import functools
 
 import numpy as np
 import scipy.sparse as sp
@@ -108,6 +109,7 @@ def _eval_v(k, lvl, cell, mode, x):
     return np.sqrt(float(1 << lvl)) * val * (np.abs(y) <= 1)
 
 
+@functools.lru_cache(maxsize=64)
 def _pieces_1d(k, n, q, hmax=1.0 / 16):
     """Per 1D block: quadrature nodes/weights on its polynomial pieces (split
     further into sub-intervals no wider than hmax) and the basis values there.
@@ -202,24 +204,28 @@ def tensor_construct(D, k, n, vcoeff_array, scheme="sparse"):
 def fourier_coeffs(D, k, n, modes, scheme="sparse"):
     """Coefficients of sum_m amp * trig(2 pi a.x + phase), exactly separable:
     ``modes`` = [(a (D ints), amp, "sin"|"cos", phase), ...]."""
-    L, C, M = index_map(D, k, n, scheme)
-    idx = [_i1d(k, L[:, q], C[:, q], M[:, q]) for q in range(D)]
-    cache = {}
-
-    def e1d(a):
-        if a not in cache:
-            re = vcoeffs_1d(k, n, lambda x: np.cos(2 * np.pi * a * x), q=max(12, k + 8))
-            im = vcoeffs_1d(k, n, lambda x: np.sin(2 * np.pi * a * x), q=max(12, k + 8))
-            cache[a] = re + 1j * im
-        return cache[a]
-
-    out = np.zeros(L.shape[0])
+    idx = _index_1d(D, k, n, scheme)
+    out = np.zeros(idx[0].shape[0])
     for a, amp, kind, ph in modes:
-        z = np.exp(1j * ph) * np.ones(L.shape[0], complex)
+        z = np.exp(1j * ph) * np.ones(idx[0].shape[0], complex)
         for q in range(D):
-            z *= e1d(int(a[q]))[idx[q]]
+            z *= _fourier_1d(k, n, int(a[q]))[idx[q]]
         out += amp * (z.real if kind == "cos" else z.imag)
     return out
+
+
+@functools.lru_cache(maxsize=16)
+def _index_1d(D, k, n, scheme):
+    L, C, M = index_map(D, k, n, scheme)
+    return [_i1d(k, L[:, q], C[:, q], M[:, q]) for q in range(D)]
+
+
+@functools.lru_cache(maxsize=256)
+def _fourier_1d(k, n, a):
+    """1D coefficients of exp(2 pi i a x)."""
+    re = vcoeffs_1d(k, n, lambda x: np.cos(2 * np.pi * a * x), q=max(12, k + 8))
+    im = vcoeffs_1d(k, n, lambda x: np.sin(2 * np.pi * a * x), q=max(12, k + 8))
+    return re + 1j * im
 
 
 # ------------------------------------------------------------- operators ----
@@ -434,6 +440,19 @@ class Batch:
         y = np.empty(self.state_size(sid))
         check(lib().sgdg_batch_get_state(self._h, sid, y))
         return y
+
+    def total_size(self):
+        z = ctypes.c_int64()
+        check(lib().sgdg_batch_total_size(self._h, ctypes.byref(z)))
+        return z.value
+
+    def upload(self, ptr):
+        """All live states from host memory at address ``ptr`` (float64, id order)."""
+        check(lib().sgdg_batch_upload(self._h, ctypes.c_void_p(ptr)))
+
+    def download(self, ptr):
+        """All live states into host memory at address ``ptr`` (synchronises)."""
+        check(lib().sgdg_batch_download(self._h, ctypes.c_void_p(ptr)))
 
     def step_info(self):
         launches = ctypes.c_int64()

@@ -20,7 +20,8 @@ EXPORTS = [
     "sgdg_dlf_1d_export", "sgdg_op_create", "sgdg_op_destroy", "sgdg_op_size", "sgdg_op_nnz",
     "sgdg_op_export_csr", "sgdg_apply", "sgdg_apply_device", "sgdg_wave_evolve", "sgdg_advect_evolve",
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
-    "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_step_info",
+    "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
+    "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info",
     "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
 ]
 
@@ -81,6 +82,9 @@ def lib(build=True):
     _sig(L, "sgdg_batch_step", [_vp, _c64])
     _sig(L, "sgdg_batch_get_state", [_vp, _ci, _f64p])
     _sig(L, "sgdg_batch_state_size", [_vp, _ci, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_batch_total_size", [_vp, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_batch_upload", [_vp, _vp])
+    _sig(L, "sgdg_batch_download", [_vp, _vp])
     _sig(L, "sgdg_batch_step_info", [_vp, ctypes.POINTER(_c64), ctypes.POINTER(_cd)])
     _sig(L, "sgdg_set_hbm_budget", [_c64])
     _sig(L, "sgdg_hbm_in_use", [ctypes.POINTER(_c64)])

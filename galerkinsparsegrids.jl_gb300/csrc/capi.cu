@@ -24,6 +24,7 @@ cudaError_t launch_mf_pass(const MFTile* tiles, int ntiles, const MFSolve* solve
                            size_t smem, int grid, cudaStream_t st);
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
+cudaError_t launch_restage(const MFSolve* solves, int nsolves, cudaStream_t st);
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -270,6 +271,34 @@ class MFEngine {
     void get_state(int id, double* host) {
         SolveState& s = at(id);
         CK(cudaMemcpyAsync(host, s.y.p, sizeof(double) * s.Ns, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+
+    int64_t total_size() const {
+        int64_t t = 0;
+        for (auto& s : solves_)
+            if (s->live) t += s->Ns;
+        return t;
+    }
+
+    void upload_all(const double* host) {
+        plan();
+        int64_t off = 0;
+        for (auto& s : solves_) {
+            if (!s->live) continue;
+            CK(cudaMemcpyAsync(s->y.p, host + off, sizeof(double) * s->Ns, cudaMemcpyHostToDevice, stream_));
+            off += s->Ns;
+        }
+        CK(launch_restage(solves_d_.as<MFSolve>(), (int)solves_.size(), stream_));
+    }
+
+    void download_all(double* host) {
+        int64_t off = 0;
+        for (auto& s : solves_) {
+            if (!s->live) continue;
+            CK(cudaMemcpyAsync(host + off, s->y.p, sizeof(double) * s->Ns, cudaMemcpyDeviceToHost, stream_));
+            off += s->Ns;
+        }
         CK(cudaStreamSynchronize(stream_));
     }
 
@@ -897,6 +926,30 @@ int sgdg_batch_state_size(sgdg_batch* b, int id, int64_t* len) {
     NEED(b);
     NEED(len);
     *len = b->eng.at(id).Ns;
+    API_END
+}
+
+int sgdg_batch_total_size(sgdg_batch* b, int64_t* len) {
+    API_BEGIN
+    NEED(b);
+    NEED(len);
+    *len = b->eng.total_size();
+    API_END
+}
+
+int sgdg_batch_upload(sgdg_batch* b, const double* y_all) {
+    API_BEGIN
+    NEED(b);
+    NEED(y_all);
+    b->eng.upload_all(y_all);
+    API_END
+}
+
+int sgdg_batch_download(sgdg_batch* b, double* y_all) {
+    API_BEGIN
+    NEED(b);
+    NEED(y_all);
+    b->eng.download_all(y_all);
     API_END
 }
 

@@ -239,7 +239,27 @@ __global__ void k_f32_to_f64(const float* __restrict__ a, double* __restrict__ b
         b[i] = (double)a[i];
 }
 
+// stage input of every live solve from its FP64 state: u[0] = fp32(y)
+__global__ void k_restage(const MFSolve* __restrict__ solves, int nsolves) {
+    const int si = blockIdx.y;
+    if (si >= nsolves) return;
+    const MFSolve& s = solves[si];
+    if (s.status != 0) return;
+    const int64_t n = s.kind == MF_KIND_WAVE ? 2 * s.N : s.N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s.u[0][i] = (float)s.y[i];
+}
+
 // ------------------------------------------------------------ launchers ----
+cudaError_t launch_restage(const MFSolve* solves, int nsolves, cudaStream_t st) {
+    if (nsolves <= 0) return cudaSuccess;
+    for (int s0 = 0; s0 < nsolves; s0 += 65535) {
+        int cnt = nsolves - s0 < 65535 ? nsolves - s0 : 65535;
+        k_restage<<<dim3(64, cnt), 256, 0, st>>>(solves + s0, cnt);
+    }
+    return cudaGetLastError();
+}
+
 static int grid_for(int64_t threads) {
     int64_t b = (threads + 255) / 256;
     return (int)(b > (1LL << 30) ? (1LL << 30) : (b < 1 ? 1 : b));

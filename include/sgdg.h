@@ -124,6 +124,15 @@ int sgdg_batch_step(sgdg_batch *b, int64_t nsteps);
 int sgdg_batch_get_state(sgdg_batch *b, int id, double *y);
 /* Number of stored state coefficients of solve `id` (N or 2N). */
 int sgdg_batch_state_size(sgdg_batch *b, int id, int64_t *len);
+/* Sum of state sizes over the live solves. */
+int sgdg_batch_total_size(sgdg_batch *b, int64_t *len);
+/* Replaces every live solve's state from one host array (solves concatenated
+ * in increasing id order; page-locked memory makes the copies asynchronous,
+ * the caller keeps it valid until the next synchronising call). */
+int sgdg_batch_upload(sgdg_batch *b, const double *y_all);
+/* Copies every live solve's state into one host array (same order) and
+ * synchronises the batch stream. */
+int sgdg_batch_download(sgdg_batch *b, double *y_all);
 /* Launch statistics of one batch step: kernel launches and algorithmic bytes
  * (32 B per state coefficient per RK stage). */
 int sgdg_batch_step_info(sgdg_batch *b, int64_t *launches_per_step, double *dof_updates_per_step);
