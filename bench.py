@@ -204,7 +204,9 @@ def run_ours(args):
     import __graft_entry__ as g
     sg = g.load_package()
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated (non-default) stream: the library launches on it and the
+    # CUDA events below are recorded on it
+    stream = torch.cuda.Stream(device=dev)
 
     states = initial_states(sg, args.solves, 1000 + 100000 * rank)
     b = sg.Batch()
