@@ -46,8 +46,8 @@ BYTES_PER_DOF_UPDATE = 32.0  # read u fp32 + write u fp32 + read y fp64 + r/w ac
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--solves", type=int, default=256)
     p.add_argument("--e2e-steps", type=int, default=5)
