@@ -1,18 +1,18 @@
-// capi.cu -- the C ABI of libsgdg (include/sgdg.h) and its host drivers.
+// capi.cu -- the C ABI of libsgdg (include/sgdg.h).
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
-#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/sgdg.h"
+#include "device_util.h"
 #include "engine.h"
+#include "mf_engine.h"
 #include "sgdg_core.h"
 
 namespace sgdg {
@@ -20,90 +20,9 @@ namespace sgdg {
 cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st);
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
                            int stage, cudaStream_t st);
-cudaError_t launch_mf_pass(const MFTile* tiles, int ntiles, const MFSolve* solves, int stage, int in_sel, int rk,
-                           size_t smem, int grid, cudaStream_t st);
-cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
-cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
-cudaError_t launch_restage(const MFSolve* solves, int nsolves, cudaStream_t st);
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
-
-#define CK(call)                                                                                        \
-    do {                                                                                                \
-        cudaError_t e_ = (call);                                                                        \
-        if (e_ != cudaSuccess)                                                                          \
-            throw Error(e_ == cudaErrorMemoryAllocation ? SGDG_ENOMEM_BUDGET : SGDG_ECUDA,             \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
-    } while (0)
-
-// ------------------------------------------------------------ device ----
-static void require_gpu() {
-    static int state = -1;  // -1 unknown, 0 none, 1 ok
-    if (state == 1) return;
-    int n = 0;
-    cudaError_t e = cudaGetDeviceCount(&n);
-    if (e != cudaSuccess || n == 0) {
-        cudaGetLastError();
-        state = 0;
-        throw Error(SGDG_ENOGPU, std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
-    }
-    state = 1;
-}
-
-static std::atomic<int64_t> g_budget{0}, g_in_use{0};
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    DevBuf() = default;
-    explicit DevBuf(size_t n) { alloc(n); }
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
-    DevBuf& operator=(DevBuf&& o) noexcept {
-        release();
-        p = o.p;
-        bytes = o.bytes;
-        o.p = nullptr;
-        o.bytes = 0;
-        return *this;
-    }
-    void alloc(size_t n) {
-        release();
-        if (n == 0) n = 16;
-        int64_t b = g_budget.load();
-        if (b > 0 && g_in_use.load() + (int64_t)n > b)
-            throw Error(SGDG_ENOMEM_BUDGET, "HBM budget exceeded: requested " + std::to_string(n) + " bytes, " +
-                                                std::to_string(g_in_use.load()) + " of " + std::to_string(b) + " in use");
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            p = nullptr;
-            throw Error(SGDG_ENOMEM_BUDGET, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        }
-        bytes = n;
-        g_in_use += (int64_t)n;
-    }
-    void release() {
-        if (p) {
-            cudaFree(p);
-            g_in_use -= (int64_t)bytes;
-        }
-        p = nullptr;
-        bytes = 0;
-    }
-    ~DevBuf() { release(); }
-    template <class T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-template <class T>
-static DevBuf upload(const std::vector<T>& v, cudaStream_t st) {
-    DevBuf b(v.size() * sizeof(T));
-    if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
-    return b;
-}
 
 // ------------------------------------------------------- plain form ----
 struct DeviceCSR {
@@ -134,309 +53,6 @@ static std::unique_ptr<DeviceCSR> to_device(const CSR& A, cudaStream_t st) {
     D->d.vs = pick_vs(A);
     return D;
 }
-
-// ------------------------------------------------- matrix-free engine ----
-struct SolveSpec {
-    int kind, D, k, n, scheme;
-    double a[8];
-    double dt;
-    int apply_dim;  // -1: all dimensions; else only this 0-based dimension (apply mode)
-};
-
-struct STable {  // 1D operator in FP32 block CSR on the device
-    DevBuf rowptr, colblk, val;
-};
-
-struct SolveState {
-    SolveSpec spec;
-    SparseIndex ix;
-    int64_t N = 0, Ns = 0;
-    DevBuf y, acc, u0, u1, rhs, boff;
-    std::vector<int64_t> boff_h;
-    std::vector<MFTile> tiles;  // solve index filled at plan time
-    bool live = true;
-};
-
-static constexpr int kTileElems = 4096;
-
-class MFEngine {
-   public:
-    explicit MFEngine(cudaStream_t st = nullptr) : stream_(st) {}
-    ~MFEngine() { drop_graph(); }
-
-    void set_stream(cudaStream_t st) {
-        if (st != stream_) drop_graph();
-        stream_ = st;
-    }
-    cudaStream_t stream() const { return stream_; }
-
-    int add(const SolveSpec& sp, const double* y0_host, bool y0_device = false) {
-        require_gpu();
-        auto s = std::make_unique<SolveState>();
-        s->spec = sp;
-        s->ix = make_index(sp.D, sp.k, sp.n, sp.scheme);
-        if (sp.k > 5) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports k <= 5 (use the plain form)");
-        auto op = dlf1d(sp.k, sp.n);
-        stab(sp.k, sp.n, *op);
-        s->N = s->ix.N;
-        s->Ns = sp.kind == MF_KIND_WAVE ? 2 * s->N : s->N;
-        // pencils and tiles
-        for (int d = 0; d < sp.D; d++) {
-            if (sp.apply_dim >= 0 && d != sp.apply_dim) continue;
-            auto pens = make_pencils(s->ix, d);
-            int kd1 = 1, kDm1 = 1;
-            for (int q = 0; q < d; q++) kd1 *= sp.k;
-            for (int q = 0; q < sp.D - 1; q++) kDm1 *= sp.k;
-            for (const auto& p : pens) {
-                int32_t boff = (int32_t)s->boff_h.size();
-                for (auto o : p.blockoff) s->boff_h.push_back(o);
-                int64_t m = int64_t(sp.k) << (p.lmax - 1);
-                int64_t wc = std::max<int64_t>(1, std::min<int64_t>(p.R, kTileElems / m));
-                for (int64_t r0 = 0; r0 < p.R; r0 += wc) {
-                    MFTile t{};
-                    t.d = (int16_t)d;
-                    int first_d = sp.apply_dim >= 0 ? sp.apply_dim : 0;
-                    int last_d = sp.apply_dim >= 0 ? sp.apply_dim : sp.D - 1;
-                    t.flags = (int16_t)((d == first_d ? TILE_FIRST : 0) | (d == last_d ? TILE_LAST : 0));
-                    t.lmax = p.lmax;
-                    t.lp = p.lp;
-                    t.boff = boff;
-                    t.r0 = (int32_t)r0;
-                    t.wc = (int32_t)std::min<int64_t>(wc, p.R - r0);
-                    t.kd1 = kd1;
-                    t.kDm1 = kDm1;
-                    s->tiles.push_back(t);
-                }
-            }
-        }
-        s->y.alloc(sizeof(double) * s->Ns);
-        s->acc.alloc(sizeof(double) * s->Ns);
-        s->u0.alloc(sizeof(float) * s->Ns);
-        s->u1.alloc(sizeof(float) * s->Ns);
-        s->rhs.alloc(sizeof(float) * s->N);
-        s->boff = upload(s->boff_h, stream_);
-        if (y0_host) {
-            if (y0_device)
-                CK(cudaMemcpyAsync(s->y.p, y0_host, sizeof(double) * s->Ns, cudaMemcpyDeviceToDevice, stream_));
-            else
-                CK(cudaMemcpyAsync(s->y.p, y0_host, sizeof(double) * s->Ns, cudaMemcpyHostToDevice, stream_));
-            CK(launch_f64_to_f32(s->y.as<double>(), s->u0.as<float>(), s->Ns, stream_));
-        }
-        solves_.push_back(std::move(s));
-        dirty_ = true;
-        return (int)solves_.size() - 1;
-    }
-
-    void remove(int id) {
-        SolveState& s = at(id);
-        CK(cudaStreamSynchronize(stream_));
-        s.live = false;
-        s.y.release();
-        s.acc.release();
-        s.u0.release();
-        s.u1.release();
-        s.rhs.release();
-        s.boff.release();
-        s.tiles.clear();
-        dirty_ = true;
-    }
-
-    SolveState& at(int id) {
-        if (id < 0 || id >= (int)solves_.size() || !solves_[id]->live) throw Error(SGDG_EINVAL, "no such solve id");
-        return *solves_[id];
-    }
-
-    // u[0] <- fp32(x) for apply mode (x on device, N values)
-    void load_input_device(int id, const double* x_dev) {
-        SolveState& s = at(id);
-        CK(launch_f64_to_f32(x_dev, s.u0.as<float>(), s.N, stream_));
-    }
-
-    void run_apply(double* y_dev) {
-        plan();
-        for (int p = 0; p < dmax_; p++)
-            CK(launch_mf_pass(tiles_d_.as<MFTile>() + pass_begin_[p], pass_begin_[p + 1] - pass_begin_[p],
-                              solves_d_.as<MFSolve>(), 1, 0, 0, smem_, 0, stream_));
-        SolveState& s = *solves_[0];
-        CK(launch_f32_to_f64(s.rhs.as<float>(), y_dev, s.N, stream_));
-    }
-
-    void step(int64_t nsteps) {
-        plan();
-        if (ntiles_ == 0 || nsteps <= 0) return;
-        if (!graph_) capture();
-        for (int64_t i = 0; i < nsteps; i++) CK(cudaGraphLaunch(graph_, stream_));
-    }
-
-    void get_state(int id, double* host) {
-        SolveState& s = at(id);
-        CK(cudaMemcpyAsync(host, s.y.p, sizeof(double) * s.Ns, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaStreamSynchronize(stream_));
-    }
-
-    int64_t total_size() const {
-        int64_t t = 0;
-        for (auto& s : solves_)
-            if (s->live) t += s->Ns;
-        return t;
-    }
-
-    void upload_all(const double* host) {
-        plan();
-        int64_t off = 0;
-        for (auto& s : solves_) {
-            if (!s->live) continue;
-            CK(cudaMemcpyAsync(s->y.p, host + off, sizeof(double) * s->Ns, cudaMemcpyHostToDevice, stream_));
-            off += s->Ns;
-        }
-        CK(launch_restage(solves_d_.as<MFSolve>(), (int)solves_.size(), stream_));
-    }
-
-    void download_all(double* host) {
-        int64_t off = 0;
-        for (auto& s : solves_) {
-            if (!s->live) continue;
-            CK(cudaMemcpyAsync(host + off, s->y.p, sizeof(double) * s->Ns, cudaMemcpyDeviceToHost, stream_));
-            off += s->Ns;
-        }
-        CK(cudaStreamSynchronize(stream_));
-    }
-
-    double dof_updates_per_step() const {
-        double t = 0;
-        for (auto& s : solves_)
-            if (s->live) t += 4.0 * double(s->Ns);
-        return t;
-    }
-    int64_t launches_per_step() const {
-        int dm = 0;
-        for (auto& s : solves_)
-            if (s->live) dm = std::max(dm, s->spec.apply_dim >= 0 ? 1 : s->spec.D);
-        return 4LL * dm;
-    }
-    size_t smem() const { return smem_; }
-
-   private:
-    void stab(int k, int n, const DLF1D& op) {
-        auto key = std::make_pair(k, n);
-        if (stabs_.count(key)) return;
-        const int kk = ((k * k + 3) / 4) * 4;
-        std::vector<float> v((size_t)op.colblk.size() * kk, 0.f);
-        for (size_t b = 0; b < op.colblk.size(); b++)
-            for (int t = 0; t < k * k; t++) v[b * kk + t] = (float)op.val[b * k * k + t];
-        STable S;
-        S.rowptr = upload(op.rowptr, stream_);
-        S.colblk = upload(op.colblk, stream_);
-        S.val = upload(v, stream_);
-        stabs_.emplace(key, std::move(S));
-    }
-
-    void plan() {
-        if (!dirty_) return;
-        drop_graph();
-        std::vector<MFSolve> sh;
-        std::vector<std::vector<MFTile>> per_pass(kDMax);
-        dmax_ = 0;
-        size_t smem = 0;
-        for (size_t i = 0; i < solves_.size(); i++) {
-            SolveState& s = *solves_[i];
-            MFSolve m{};
-            if (s.live) {
-                const STable& S = stabs_.at({s.spec.k, s.spec.n});
-                m.y = s.y.as<double>();
-                m.acc = s.acc.as<double>();
-                m.u[0] = s.u0.as<float>();
-                m.u[1] = s.u1.as<float>();
-                m.rhs = s.rhs.as<float>();
-                m.s_rowptr = S.rowptr.as<int32_t>();
-                m.s_colblk = S.colblk.as<int32_t>();
-                m.s_val = S.val.as<float>();
-                m.blockoff = s.boff.as<int64_t>();
-                m.dt = s.spec.dt;
-                m.N = s.N;
-                m.D = s.spec.D;
-                m.k = s.spec.k;
-                m.kk = ((s.spec.k * s.spec.k + 3) / 4) * 4;
-                m.kind = s.spec.kind;
-                int kD = 1;
-                for (int q = 0; q < s.spec.D; q++) kD *= s.spec.k;
-                m.kD = kD;
-                m.status = 0;
-                for (int d = 0; d < 8; d++)
-                    m.coef[d] = (float)(s.spec.kind == MF_KIND_WAVE ? 1.0 : (s.spec.apply_dim >= 0 ? 1.0 : -s.spec.a[d]));
-                int pass = 0;
-                for (auto t : s.tiles) {
-                    t.solve = (int32_t)i;
-                    pass = s.spec.apply_dim >= 0 ? 0 : t.d;
-                    per_pass[pass].push_back(t);
-                    int64_t mrows = int64_t(s.spec.k) << (t.lmax - 1);
-                    size_t b = 4 * (2 * (size_t)t.wc + (size_t)(mrows * t.wc) * (s.spec.kind == MF_KIND_WAVE ? 2 : 1));
-                    smem = std::max(smem, b);
-                    dmax_ = std::max(dmax_, pass + 1);
-                }
-            } else {
-                m.status = 1;
-            }
-            sh.push_back(m);
-        }
-        if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "pencil tile exceeds shared memory");
-        smem_ = smem;
-        std::vector<MFTile> all;
-        pass_begin_.assign(1, 0);
-        for (int p = 0; p < dmax_; p++) {
-            all.insert(all.end(), per_pass[p].begin(), per_pass[p].end());
-            pass_begin_.push_back((int)all.size());
-        }
-        ntiles_ = (int)all.size();
-        solves_d_ = upload(sh, stream_);
-        tiles_d_ = upload(all, stream_);
-        CK(cudaStreamSynchronize(stream_));
-        dirty_ = false;
-    }
-
-    void capture() {
-        cudaStream_t cs = stream_;
-        cudaStream_t own = nullptr;
-        if (cs == nullptr) {  // graphs cannot be captured on the legacy stream
-            CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
-            cs = own;
-        }
-        cudaGraph_t g = nullptr;
-        CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        cudaError_t err = cudaSuccess;
-        for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
-            for (int p = 0; p < dmax_ && err == cudaSuccess; p++)
-                err = launch_mf_pass(tiles_d_.as<MFTile>() + pass_begin_[p], pass_begin_[p + 1] - pass_begin_[p],
-                                     solves_d_.as<MFSolve>(), stage, (stage - 1) % 2, 1, smem_, 0, cs);
-        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-        if (own) cudaStreamDestroy(own);
-        if (err != cudaSuccess || e2 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            throw Error(SGDG_ECUDA, std::string("graph capture: ") + cudaGetErrorString(err != cudaSuccess ? err : e2));
-        }
-        cudaError_t e3 = cudaGraphInstantiate(&graph_, g, 0);
-        cudaGraphDestroy(g);
-        if (e3 != cudaSuccess) {
-            graph_ = nullptr;
-            throw Error(SGDG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
-        }
-    }
-
-    void drop_graph() {
-        if (graph_) cudaGraphExecDestroy(graph_);
-        graph_ = nullptr;
-    }
-
-    cudaStream_t stream_ = nullptr;
-    std::vector<std::unique_ptr<SolveState>> solves_;
-    std::map<std::pair<int, int>, STable> stabs_;
-    DevBuf solves_d_, tiles_d_;
-    std::vector<int> pass_begin_;
-    int dmax_ = 0, ntiles_ = 0;
-    size_t smem_ = 0;
-    bool dirty_ = true;
-    cudaGraphExec_t graph_ = nullptr;
-};
 
 }  // namespace sgdg
 
@@ -684,13 +300,13 @@ static void apply_device_impl(sgdg_op* op, int which, int method, const double* 
         sp.n = op->ix.n;
         sp.scheme = op->ix.scheme;
         sp.dt = 0.0;
+        sp.apply = true;
         sp.apply_dim = which >= 1 ? which - 1 : -1;
         eng->add(sp, nullptr);
         it = op->mf_apply.emplace(which, std::move(eng)).first;
     }
     it->second->set_stream(st);
-    it->second->load_input_device(0, x);
-    it->second->run_apply(y);
+    it->second->apply(x, y);
 }
 
 int sgdg_apply(sgdg_op* op, int which, int method, const double* x, double* y) {
@@ -925,7 +541,7 @@ int sgdg_batch_state_size(sgdg_batch* b, int id, int64_t* len) {
     API_BEGIN
     NEED(b);
     NEED(len);
-    *len = b->eng.at(id).Ns;
+    *len = b->eng.state_size(id);
     API_END
 }
 

@@ -16,39 +16,53 @@ struct DevCSR {
 };
 
 // ---- chosen form: matrix-free FP32 pencil apply, FP64 RK state --------------
+//
+// Solves with equal (D, k, n, scheme, kind) form a class.  A class keeps its
+// solves' vectors in arenas (slot-major: slot s owns [s*Ns, (s+1)*Ns)), so a
+// tile may take columns from several solves.  One launch per RK stage runs an
+// ordered work list: for every group of slots, one pass per dimension (pencil
+// tiles: sweep the 1D operator, accumulate into rhs) and then the RK update
+// of the group; each phase waits for the previous phase of its group.
 enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1 };
 enum : int { TILE_FIRST = 1, TILE_LAST = 2 };
+enum : int { ITEM_PASS = 0, ITEM_RK = 1 };
 
-struct MFSolve {
-    double* y;       // RK state (N or 2N for the wave)
-    double* acc;     // RK accumulator
-    float* u[2];     // stage inputs/outputs (ping-pong), same length as y
-    float* rhs;      // partial sum over dimensions, N
+struct MFClass {
     const int32_t* s_rowptr;  // 1D operator, block CSR over 2^n row blocks
     const int32_t* s_colblk;
-    const float* s_val;       // blocks of kk floats, [i][j] row-major
-    const int64_t* blockoff;  // pencil level-block offsets (all pencils of this solve)
-    double dt;
-    int64_t N;       // operator size (coefficients per field)
-    int D, k, kk, kind;
-    int kD;          // k^D
-    int status;      // nonzero once the solve is stopped (cancel / error)
-    float coef[8];   // factor on D_d (advection: -a_d; wave: 1)
+    const float* s_val;       // per block: k rows of (hi, lo) pairs, each row padded to rs floats
+    const int64_t* blockoff;  // level-block offsets of every pencil of the class
+    double* y;                // arenas, nslots * Ns
+    double* acc;
+    float* u[2];
+    float* rhs;               // nslots * N
+    const double* dt;         // per slot
+    const float* coef;        // per slot, 8 entries: factor on D_d
+    const int32_t* status;    // per slot, nonzero = skip the RK update
+    int32_t N, Ns;
+    int32_t D, k, kD, kind, rs;
 };
 
-struct MFTile {
-    int32_t solve;
-    int16_t d;       // 0-based dimension
-    int16_t flags;   // TILE_FIRST | TILE_LAST
-    int32_t lmax;    // 1-based max level of the pencil along d
-    int32_t lp;      // log2 prod_{q<d} cells_q
-    int32_t boff;    // index of the pencil's first level-block offset in blockoff
-    int32_t r0;      // first column of the chunk
-    int32_t wc;      // columns in the chunk
-    int32_t kd1;     // k^d (stride of dimension d's mode)
-    int32_t kDm1;    // k^(D-1)
+struct MFItem {
+    int16_t type;      // ITEM_PASS / ITEM_RK
+    int16_t cls;
+    int16_t d;         // pass: 0-based dimension
+    int16_t flags;     // pass: TILE_FIRST | TILE_LAST
+    int32_t wait_ctr;  // counter to wait for (-1: none) ...
+    int32_t wait_need; // ... until it reaches this value
+    int32_t done_ctr;  // counter incremented when the item is done
+    int32_t lmax;      // pass: 1-based max level of the pencil along d
+    int32_t lp;        // pass: log2 prod_{q<d} cells_q
+    int32_t boff;      // pass: first level-block offset of the pencil in blockoff
+    int32_t R;         // pass: columns per solve;  RK: slot
+    int32_t g0;        // pass: first class column (slot*R + r);  RK: first element
+    int32_t W;         // pass: columns (multiple of the per-thread column count);  RK: end element
+    int32_t Wv;        // pass: valid columns
+    int32_t kd1;       // pass: k^d
+    int32_t kDm1;      // pass: k^(D-1)
 };
 
 constexpr int kMFThreads = 256;
+constexpr int kSpinLimit = 1 << 22;  // polls of a dependency counter before giving up
 
 }  // namespace sgdg

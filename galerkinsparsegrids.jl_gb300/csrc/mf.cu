@@ -1,0 +1,330 @@
+// mf.cu -- the matrix-free form: one persistent launch per RK4 stage.
+//
+// The launch walks an ordered work list (engine.h): for each group of solves
+// of a class, one pass per dimension d and then the group's RK update.  A
+// pass item is a pencil tile: the pencil's 1D prefix (m = k 2^(lmax-1) rows)
+// times W columns taken across the group's solves.  The tile is gathered into
+// shared memory with cp.async, swept with the 1D operator's k x k blocks
+// (stored as FP32 hi + lo pairs and applied with the paired FMA __ffma2_rn,
+// so the operator carries ~FP64 entries while the data stays FP32), and the
+// result is added into the FP32 partial-sum vector rhs (L2-resident for the
+// group, accessed with .cg so other SMs' writes are seen).  For the wave
+// (u_tt = sum_d D_d D_d u) the tile applies the 1D operator twice.  The RK
+// item streams the group's FP64 state once: k from rhs (and, for the wave's
+// displacement field, from the stage input of the velocity field), then the
+// stage combination and the FP32 stage input of the next stage.
+//
+// Ordering: items are handed out in list order by an atomic counter; an item
+// of phase p waits (bounded spin) until every item of phase p-1 of its group
+// has finished, so progress never depends on a later item.  A wait that runs
+// out sets *err and skips the item.
+#include <cuda_runtime.h>
+
+#include "engine.h"
+#include "rk.cuh"
+
+namespace sgdg {
+
+__device__ __forceinline__ int block_level(int rb) { return rb == 0 ? 1 : (32 - __clz(rb)) + 1; }
+
+__device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+struct TileCols {  // per-column tables in shared memory
+    const int* slot;  // solve slot of the column (-1: padding)
+    const int* a;     // offset within the solve of the column's row-0 element, low part
+    const int* b;     // high cell part, shifted left by the row's level
+};
+
+template <int K>
+__device__ __forceinline__ int elem_off(const int* __restrict__ boff, const TileCols& cols, int kD, int lp, int kd1,
+                                        int rb, int i, int j) {
+    const int l = block_level(rb);
+    const int lc = l > 2 ? l - 2 : 0;
+    const int cd0 = l >= 2 ? rb - (1 << (l - 2)) : 0;
+    return boff[l - 1] + cols.a[j] + (cols.b[j] << lc) + kD * (cd0 << lp) + i * kd1;
+}
+
+// acc[i][c] += S(rb, cb)[i][jj] * src[cb*K + jj][jq*CPT + c] over the stored
+// blocks of row block rb with cb < nrb; S = hi + lo (two FP32 accumulators).
+template <int K, int CPT>
+__device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict__ src, int W, int nrb, int rb, int jq,
+                                      float (&out)[K][CPT]) {
+    constexpr int RS = ((2 * K + 3) / 4) * 4;
+    float2 acc[K][CPT];
+#pragma unroll
+    for (int i = 0; i < K; i++)
+#pragma unroll
+        for (int c = 0; c < CPT; c++) acc[i][c] = make_float2(0.f, 0.f);
+    const int pb = __ldg(C.s_rowptr + rb), pe = __ldg(C.s_rowptr + rb + 1);
+    for (int p = pb; p < pe; ++p) {
+        const int cb = __ldg(C.s_colblk + p);
+        if (cb >= nrb) break;
+        float x[K][CPT];
+#pragma unroll
+        for (int jj = 0; jj < K; jj++) {
+            const float* xp = src + (cb * K + jj) * W + jq * CPT;
+            if constexpr (CPT == 4) {
+                const float4 v = *reinterpret_cast<const float4*>(xp);
+                x[jj][0] = v.x;
+                x[jj][1] = v.y;
+                x[jj][2] = v.z;
+                x[jj][3] = v.w;
+            } else {
+                const float2 v = *reinterpret_cast<const float2*>(xp);
+                x[jj][0] = v.x;
+                x[jj][1] = v.y;
+            }
+        }
+        const float4* sv = reinterpret_cast<const float4*>(C.s_val + (size_t)p * (K * RS));
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            float srow[RS];
+#pragma unroll
+            for (int v = 0; v < RS / 4; v++) {
+                const float4 f = __ldg(sv + i * (RS / 4) + v);
+                srow[4 * v] = f.x;
+                srow[4 * v + 1] = f.y;
+                srow[4 * v + 2] = f.z;
+                srow[4 * v + 3] = f.w;
+            }
+#pragma unroll
+            for (int jj = 0; jj < K; jj++) {
+                const float2 s = make_float2(srow[2 * jj], srow[2 * jj + 1]);
+#pragma unroll
+                for (int c = 0; c < CPT; c++) acc[i][c] = __ffma2_rn(s, make_float2(x[jj][c], x[jj][c]), acc[i][c]);
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < K; i++)
+#pragma unroll
+        for (int c = 0; c < CPT; c++) out[i][c] = acc[i][c].x + acc[i][c].y;
+}
+
+template <int K, int CPT, bool WAVE>
+__device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float* smem) {
+    const int tid = threadIdx.x;
+    const int nrb = 1 << (it.lmax - 1);
+    const int m = nrb * K;
+    const int W = it.W, Wv = it.Wv;
+    const int lw = __ffs(W) - 1;  // W is a power of two
+    int* cslot = reinterpret_cast<int*>(smem);
+    int* ca = cslot + W;
+    int* cb = ca + W;
+    float* X = reinterpret_cast<float*>(cb + W);  // 12W bytes in: 16-aligned for W % 4 == 0, 8 for W % 2 == 0
+    float* Y = X + m * W;
+    const int kD = C.kD, kd1 = it.kd1, lp = it.lp, R = it.R, kDm1 = it.kDm1;
+    for (int j = tid; j < W; j += kMFThreads) {
+        if (j < Wv) {
+            const int g = it.g0 + j;
+            const int slot = g / R, r = g - slot * R;
+            const int mr = r % kDm1, cr = r / kDm1;
+            cslot[j] = slot;
+            ca[j] = kD * (cr & ((1 << lp) - 1)) + (mr % kd1) + (mr / kd1) * kd1 * K;
+            cb[j] = kD * ((cr >> lp) << lp);
+        } else {
+            cslot[j] = -1;
+            ca[j] = 0;
+            cb[j] = 0;
+        }
+    }
+    __syncthreads();
+    const TileCols cols{cslot, ca, cb};
+    const int64_t* __restrict__ pboff = C.blockoff + it.boff;
+    // level-block offsets of the pencil fit in int (N < 2^31)
+    __shared__ int sboff[32];
+    if (tid < it.lmax) sboff[tid] = (int)pboff[tid];
+    __syncthreads();
+    const float* __restrict__ uin = C.u[in_sel];
+    const int ne = m << lw;
+    for (int e = tid; e < ne; e += kMFThreads) {
+        const int row = e >> lw, j = e & (W - 1);
+        const int s = cslot[j];
+        if (s < 0) {
+            X[e] = 0.f;
+            continue;
+        }
+        const int rb = row / K, i = row - rb * K;
+        cp_async4(X + e, uin + (size_t)s * C.Ns + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j));
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int lwq = lw - (CPT == 4 ? 2 : 1);
+    const int nq = nrb << lwq;
+    if (WAVE) {
+        for (int q = tid; q < nq; q += kMFThreads) {
+            const int rb = q >> lwq, jq = q & ((1 << lwq) - 1);
+            float o[K][CPT];
+            sweep<K, CPT>(C, X, W, nrb, rb, jq, o);
+#pragma unroll
+            for (int i = 0; i < K; i++) {
+                float* yp = Y + (rb * K + i) * W + jq * CPT;
+                if constexpr (CPT == 4)
+                    *reinterpret_cast<float4*>(yp) = make_float4(o[i][0], o[i][1], o[i][2], o[i][3]);
+                else
+                    *reinterpret_cast<float2*>(yp) = make_float2(o[i][0], o[i][1]);
+            }
+        }
+        __syncthreads();
+    }
+    const bool first = (it.flags & TILE_FIRST) != 0;
+    for (int q = tid; q < nq; q += kMFThreads) {
+        const int rb = q >> lwq, jq = q & ((1 << lwq) - 1);
+        float o[K][CPT];
+        sweep<K, CPT>(C, WAVE ? Y : X, W, nrb, rb, jq, o);
+        // element offsets of the quad in the rhs arena (-1: padding column)
+        int off[K][CPT];
+#pragma unroll
+        for (int c = 0; c < CPT; c++) {
+            const int j = jq * CPT + c;
+            const int s = cslot[j];
+            const float coef = s >= 0 ? __ldg(C.coef + s * 8 + it.d) : 0.f;
+            const int e0 = s >= 0 ? s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, 0, j) : -1;
+#pragma unroll
+            for (int i = 0; i < K; i++) {
+                off[i][c] = e0 < 0 ? -1 : e0 + i * kd1;
+                o[i][c] *= coef;
+            }
+        }
+        if (!first) {
+#pragma unroll
+            for (int c = 0; c < CPT; c++)
+#pragma unroll
+                for (int i = 0; i < K; i++)
+                    if (off[i][c] >= 0) o[i][c] += __ldcg(C.rhs + off[i][c]);
+        }
+#pragma unroll
+        for (int c = 0; c < CPT; c++)
+#pragma unroll
+            for (int i = 0; i < K; i++)
+                if (off[i][c] >= 0) __stcg(C.rhs + off[i][c], o[i][c]);
+    }
+}
+
+__device__ void rk_chunk(const MFItem& it, const MFClass& C, int stage, int in_sel) {
+    const int slot = it.R;
+    if (C.status[slot] != 0) return;
+    const double dt = C.dt[slot];
+    const size_t base = (size_t)slot * C.Ns;
+    double* __restrict__ y = C.y + base;
+    double* __restrict__ acc = C.acc + base;
+    const float* __restrict__ uin = C.u[in_sel] + base;
+    float* __restrict__ uout = C.u[in_sel ^ 1] + base;
+    const float* rhs = C.rhs + (size_t)slot * C.N;
+    const int N = C.N;
+    const bool wave = C.kind == MF_KIND_WAVE;
+    for (int e0 = it.g0 + (int)threadIdx.x; e0 < it.W; e0 += 4 * kMFThreads) {
+        double kk[4], yy[4], aa[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int e = e0 + u * kMFThreads;
+            kk[u] = yy[u] = aa[u] = 0.0;
+            if (e < it.W) {
+                kk[u] = wave ? (e < N ? (double)uin[N + e] : (double)__ldcg(rhs + (e - N))) : (double)__ldcg(rhs + e);
+                yy[u] = y[e];
+                if (stage != 1) aa[u] = acc[e];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int e = e0 + u * kMFThreads;
+            if (e < it.W) {
+                double un;
+                rk_stage(stage, dt, kk[u], yy[u], aa[u], un);
+                if (stage == 4)
+                    y[e] = yy[u];
+                else
+                    acc[e] = aa[u];
+                uout[e] = (float)un;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kMFThreads, 3)
+    k_mf_stage(const MFItem* __restrict__ items, int nitems, const MFClass* __restrict__ classes, int* ctr, int stage,
+               int in_sel, int* err) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(ctr, 1);
+        __syncthreads();
+        const int ii = s_item;
+        __syncthreads();
+        if (ii >= nitems) break;
+        const MFItem it = items[ii];
+        if (it.wait_ctr >= 0) {
+            if (tid == 0) {
+                int polls = 0;
+                while (ld_acquire(ctr + it.wait_ctr) < it.wait_need) {
+                    if (++polls > kSpinLimit || ld_relaxed(err) != 0) {
+                        atomicExch(err, 1);
+                        break;
+                    }
+                    __nanosleep(100);
+                }
+            }
+            __syncthreads();
+        }
+        const MFClass& C = classes[it.cls];
+        if (it.type == ITEM_RK) {
+            rk_chunk(it, C, stage, in_sel);
+        } else {
+            switch (C.k * 2 + C.kind) {
+                case 2: pass_tile<1, 4, false>(it, C, in_sel, smem); break;
+                case 3: pass_tile<1, 4, true>(it, C, in_sel, smem); break;
+                case 4: pass_tile<2, 4, false>(it, C, in_sel, smem); break;
+                case 5: pass_tile<2, 4, true>(it, C, in_sel, smem); break;
+                case 6: pass_tile<3, 4, false>(it, C, in_sel, smem); break;
+                case 7: pass_tile<3, 4, true>(it, C, in_sel, smem); break;
+                case 8: pass_tile<4, 2, false>(it, C, in_sel, smem); break;
+                case 9: pass_tile<4, 2, true>(it, C, in_sel, smem); break;
+                case 10: pass_tile<5, 2, false>(it, C, in_sel, smem); break;
+                case 11: pass_tile<5, 2, true>(it, C, in_sel, smem); break;
+                default: break;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(ctr + it.done_ctr, 1);
+        }
+    }
+}
+
+int mf_columns_per_thread(int k) { return k <= 3 ? 4 : 2; }
+
+cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,
+                            int in_sel, int* err, size_t smem, int grid, cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(int) * (size_t)nctr, st);
+    if (e != cudaSuccess) return e;
+    k_mf_stage<<<grid, kMFThreads, smem, st>>>(items, nitems, classes, ctr, stage, in_sel, err);
+    return cudaGetLastError();
+}
+
+cudaError_t mf_configure(size_t smem, int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(k_mf_stage, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_mf_stage, kMFThreads, smem);
+}
+
+}  // namespace sgdg

@@ -1,0 +1,473 @@
+// mf_engine.cu -- host driver of the matrix-free form.
+//
+// Solves with equal (kind, D, k, n, scheme) share a class: their vectors live
+// in class arenas (slot-major) so pencil tiles can take columns from several
+// solves.  plan() (re)builds classes, arenas and the ordered work list when
+// solves join or leave; states move into the new arenas device-to-device.
+// One RK4 step is four launches of k_mf_stage (one per stage) captured once in
+// a CUDA graph; a membership change drops the graph and the next step
+// re-captures it.
+#include <algorithm>
+#include <cstring>
+
+#include "mf_engine.h"
+
+namespace sgdg {
+
+cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,
+                            int in_sel, int* err, size_t smem, int grid, cudaStream_t st);
+cudaError_t mf_configure(size_t smem, int* blocks_per_sm);
+int mf_columns_per_thread(int k);
+cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
+cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
+
+static constexpr int64_t kGroupReuseBytes = 24LL << 20;  // L2-resident u + rhs per group
+static constexpr int kRKChunk = 8192;
+
+MFEngine::~MFEngine() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    drop_graph();
+}
+
+void MFEngine::set_stream(cudaStream_t st) {
+    if (st != stream_) drop_graph();
+    stream_ = st;
+}
+
+void MFEngine::drop_graph() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+}
+
+MFEngine::Solve& MFEngine::at(int id) {
+    if (id < 0 || id >= (int)solves_.size() || !solves_[id].live) throw Error(SGDG_EINVAL, "no such solve id");
+    return solves_[id];
+}
+const MFEngine::Solve& MFEngine::at(int id) const {
+    if (id < 0 || id >= (int)solves_.size() || !solves_[id].live) throw Error(SGDG_EINVAL, "no such solve id");
+    return solves_[id];
+}
+
+bool MFEngine::live(int id) const { return id >= 0 && id < (int)solves_.size() && solves_[id].live; }
+
+int MFEngine::add(const SolveSpec& sp, const double* y0) {
+    require_gpu();
+    if (sp.k < 1 || sp.k > 5) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports 1 <= k <= 5 (use the plain form)");
+    if (sp.D > 8) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports D <= 8");
+    Solve s;
+    s.spec = sp;
+    SparseIndex ix = make_index(sp.D, sp.k, sp.n, sp.scheme);
+    dlf1d(sp.k, sp.n);  // validates n >= 2
+    s.N = ix.N;
+    s.Ns = sp.kind == MF_KIND_WAVE && !sp.apply ? 2 * ix.N : ix.N;
+    if (y0) s.pending.assign(y0, y0 + s.Ns);
+    else s.pending.assign(s.Ns, 0.0);
+    solves_.push_back(std::move(s));
+    dirty_ = true;
+    return (int)solves_.size() - 1;
+}
+
+void MFEngine::remove(int id) {
+    at(id).live = false;
+    dirty_ = true;
+}
+
+void MFEngine::cancel(int id) {
+    Solve& s = at(id);
+    s.cancelled = true;
+    if (!dirty_ && s.cls >= 0) {
+        int one = 1;
+        CK(cudaMemcpyAsync(classes_[s.cls]->status.as<int32_t>() + s.slot, &one, sizeof(int), cudaMemcpyHostToDevice,
+                           stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+}
+
+int64_t MFEngine::state_size(int id) const { return at(id).Ns; }
+
+int64_t MFEngine::total_size() const {
+    int64_t t = 0;
+    for (auto& s : solves_)
+        if (s.live) t += s.Ns;
+    return t;
+}
+
+double MFEngine::dof_updates_per_step() const {
+    double t = 0;
+    for (auto& s : solves_)
+        if (s.live && !s.cancelled) t += 4.0 * double(s.Ns);
+    return t;
+}
+
+const MFEngine::STable& MFEngine::stab(int k, int n) {
+    auto key = std::make_pair(k, n);
+    auto it = stabs_.find(key);
+    if (it != stabs_.end()) return it->second;
+    auto op = dlf1d(k, n);
+    // per block: k rows of (hi, lo) pairs, each row padded to rs floats
+    const int rs = ((2 * k + 3) / 4) * 4;
+    const size_t nb = op->colblk.size();
+    std::vector<float> v(nb * k * rs, 0.f);
+    for (size_t b = 0; b < nb; b++)
+        for (int i = 0; i < k; i++)
+            for (int j = 0; j < k; j++) {
+                const double x = op->val[b * k * k + i * k + j];
+                const float hi = (float)x;
+                const float lo = (float)(x - (double)hi);
+                v[(b * k + i) * rs + 2 * j] = hi;
+                v[(b * k + i) * rs + 2 * j + 1] = lo;
+            }
+    STable S;
+    S.rowptr = upload(op->rowptr, stream_);
+    S.colblk = upload(op->colblk, stream_);
+    S.val = upload(v, stream_);
+    CK(cudaStreamSynchronize(stream_));
+    return stabs_.emplace(key, std::move(S)).first->second;
+}
+
+void MFEngine::plan() {
+    if (!dirty_) return;
+    drop_graph();
+    if (!err_d_.p) {
+        err_d_.alloc(sizeof(int));
+        CK(cudaMemsetAsync(err_d_.p, 0, sizeof(int), stream_));
+    }
+    // 1. classes of live solves, in id order
+    std::vector<std::unique_ptr<ClassArena>> next;
+    std::map<std::tuple<int, int, int, int, int, bool, int>, int> cls_of;
+    for (int id = 0; id < (int)solves_.size(); id++) {
+        Solve& s = solves_[id];
+        if (!s.live) continue;
+        auto key = std::make_tuple(s.spec.kind, s.spec.D, s.spec.k, s.spec.n, s.spec.scheme, s.spec.apply,
+                                   s.spec.apply_dim);
+        auto f = cls_of.find(key);
+        if (f == cls_of.end()) {
+            auto c = std::make_unique<ClassArena>();
+            c->key = key;
+            c->ix = make_index(s.spec.D, s.spec.k, s.spec.n, s.spec.scheme);
+            c->N = s.N;
+            c->Ns = s.Ns;
+            f = cls_of.emplace(key, (int)next.size()).first;
+            next.push_back(std::move(c));
+        }
+        next[f->second]->slots.push_back(id);
+    }
+    // 2. arenas, state moves, per-slot tables
+    for (size_t ci = 0; ci < next.size(); ci++) {
+        ClassArena& c = *next[ci];
+        const int ns = (int)c.slots.size();
+        if ((int64_t)ns * c.Ns >= (int64_t(1) << 31))
+            throw Error(SGDG_EUNSUPPORTED, "a class of solves holds more than 2^31 coefficients");
+        const Solve& s0 = solves_[c.slots[0]];
+        const int D = s0.spec.D;
+        std::vector<int64_t> boff;
+        for (int d = 0; d < D; d++) {
+            c.pencils.push_back(make_pencils(c.ix, d));
+            for (auto& p : c.pencils.back()) {
+                c.boff_index.push_back((int32_t)boff.size());
+                for (auto o : p.blockoff) boff.push_back(o);
+            }
+        }
+        c.blockoff = upload(boff, stream_);
+        c.y.alloc(sizeof(double) * ns * c.Ns);
+        c.acc.alloc(sizeof(double) * ns * c.Ns);
+        c.u0.alloc(sizeof(float) * ns * c.Ns);
+        c.u1.alloc(sizeof(float) * ns * c.Ns);
+        c.rhs.alloc(sizeof(float) * ns * c.N);
+        std::vector<double> dt(ns);
+        std::vector<float> coef((size_t)ns * 8, 0.f);
+        std::vector<int32_t> status(ns, 0);
+        for (int sl = 0; sl < ns; sl++) {
+            Solve& s = solves_[c.slots[sl]];
+            dt[sl] = s.spec.dt;
+            for (int d = 0; d < 8; d++)
+                coef[sl * 8 + d] =
+                    (float)(s.spec.apply || s.spec.kind == MF_KIND_WAVE ? 1.0 : -s.spec.a[d]);
+            status[sl] = s.cancelled ? 1 : 0;
+            double* dst = c.y.as<double>() + (size_t)sl * c.Ns;
+            if (!s.pending.empty()) {
+                CK(cudaMemcpyAsync(dst, s.pending.data(), sizeof(double) * c.Ns, cudaMemcpyHostToDevice, stream_));
+            } else if (s.cls >= 0) {
+                const ClassArena& old = *classes_[s.cls];
+                CK(cudaMemcpyAsync(dst, old.y.as<double>() + (size_t)s.slot * old.Ns, sizeof(double) * c.Ns,
+                                   cudaMemcpyDeviceToDevice, stream_));
+            } else {
+                CK(cudaMemsetAsync(dst, 0, sizeof(double) * c.Ns, stream_));
+            }
+        }
+        c.dt = upload(dt, stream_);
+        c.coef = upload(coef, stream_);
+        c.status = upload(status, stream_);
+        CK(launch_f64_to_f32(c.y.as<double>(), c.u0.as<float>(), (int64_t)ns * c.Ns, stream_));
+    }
+    CK(cudaStreamSynchronize(stream_));
+    // the old arenas are no longer referenced
+    classes_.swap(next);
+    next.clear();
+    for (size_t ci = 0; ci < classes_.size(); ci++)
+        for (size_t sl = 0; sl < classes_[ci]->slots.size(); sl++) {
+            Solve& s = solves_[classes_[ci]->slots[sl]];
+            s.cls = (int)ci;
+            s.slot = (int)sl;
+            s.pending.clear();
+            s.pending.shrink_to_fit();
+        }
+    for (auto& s : solves_)
+        if (!s.live) {
+            s.cls = s.slot = -1;
+        }
+    // 3. class descriptors and the work list
+    std::vector<MFClass> ch;
+    for (auto& cp : classes_) {
+        ClassArena& c = *cp;
+        const Solve& s0 = solves_[c.slots[0]];
+        const STable& S = stab(s0.spec.k, s0.spec.n);
+        MFClass m{};
+        m.s_rowptr = S.rowptr.as<int32_t>();
+        m.s_colblk = S.colblk.as<int32_t>();
+        m.s_val = S.val.as<float>();
+        m.blockoff = c.blockoff.as<int64_t>();
+        m.y = c.y.as<double>();
+        m.acc = c.acc.as<double>();
+        m.u[0] = c.u0.as<float>();
+        m.u[1] = c.u1.as<float>();
+        m.rhs = c.rhs.as<float>();
+        m.dt = c.dt.as<double>();
+        m.coef = c.coef.as<float>();
+        m.status = c.status.as<int32_t>();
+        m.N = (int32_t)c.N;
+        m.Ns = (int32_t)c.Ns;
+        m.D = s0.spec.D;
+        m.k = s0.spec.k;
+        int kD = 1;
+        for (int q = 0; q < m.D; q++) kD *= m.k;
+        m.kD = kD;
+        m.kind = s0.spec.kind;
+        m.rs = ((2 * m.k + 3) / 4) * 4;
+        ch.push_back(m);
+    }
+    std::vector<MFItem> items;
+    int nctr = 0;
+    build_items(items, nctr);
+    classes_d_ = upload(ch, stream_);
+    items_d_ = upload(items, stream_);
+    ctr_d_.alloc(sizeof(int) * (size_t)std::max(nctr, 1));
+    nitems_ = (int)items.size();
+    nctr_ = nctr;
+    int bps = 0;
+    CK(mf_configure(smem_, &bps));
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    grid_ = std::max(1, bps) * sms;
+    CK(cudaStreamSynchronize(stream_));
+    dirty_ = false;
+}
+
+void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
+    nctr = 1;  // counter 0 hands out items
+    std::vector<int> count;  // items per counter
+    count.push_back(0);
+    size_t smem = 64;
+    for (size_t ci = 0; ci < classes_.size(); ci++) {
+        ClassArena& c = *classes_[ci];
+        const SolveSpec& sp = solves_[c.slots[0]].spec;
+        const int D = sp.D, k = sp.k;
+        const bool wave = sp.kind == MF_KIND_WAVE;
+        const int cpt = mf_columns_per_thread(k);
+        std::vector<int> dims;
+        if (sp.apply && sp.apply_dim >= 0)
+            dims.push_back(sp.apply_dim);
+        else
+            for (int d = 0; d < D; d++) dims.push_back(d);
+        const int ns = (int)c.slots.size();
+        const int64_t per_solve = 8 * c.N;
+        const int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
+        int kDm1 = 1;
+        for (int q = 0; q < D - 1; q++) kDm1 *= k;
+        for (int s0 = 0; s0 < ns; s0 += gs) {
+            const int s1 = std::min(ns, s0 + gs);
+            int prev = -1;
+            for (size_t ph = 0; ph < dims.size(); ph++) {
+                const int d = dims[ph];
+                int kd1 = 1;
+                for (int q = 0; q < d; q++) kd1 *= k;
+                const int ctr = nctr++;
+                count.push_back(0);
+                int bi = 0;
+                for (int dd = 0; dd < d; dd++) bi += (int)c.pencils[dd].size();
+                for (size_t pi = 0; pi < c.pencils[d].size(); pi++) {
+                    const Pencil& p = c.pencils[d][pi];
+                    const int nrb = 1 << (p.lmax - 1);
+                    const int Wp = cpt * std::max(1, 256 / nrb);
+                    const int64_t cbeg = (int64_t)s0 * p.R, cend = (int64_t)s1 * p.R;
+                    const size_t sm = 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * (wave ? 2 : 1));
+                    smem = std::max(smem, sm);
+                    for (int64_t g0 = cbeg; g0 < cend; g0 += Wp) {
+                        MFItem it{};
+                        it.type = ITEM_PASS;
+                        it.cls = (int16_t)ci;
+                        it.d = (int16_t)d;
+                        it.flags = (int16_t)((ph == 0 ? TILE_FIRST : 0) | (ph + 1 == dims.size() ? TILE_LAST : 0));
+                        it.wait_ctr = prev;
+                        it.done_ctr = ctr;
+                        it.lmax = p.lmax;
+                        it.lp = p.lp;
+                        it.boff = c.boff_index[bi + pi];
+                        it.R = (int32_t)p.R;
+                        it.g0 = (int32_t)g0;
+                        it.W = Wp;
+                        it.Wv = (int32_t)std::min<int64_t>(Wp, cend - g0);
+                        it.kd1 = kd1;
+                        it.kDm1 = kDm1;
+                        items.push_back(it);
+                        count[ctr]++;
+                    }
+                }
+                prev = ctr;
+            }
+            if (!sp.apply) {
+                const int ctr = nctr++;
+                count.push_back(0);
+                for (int sl = s0; sl < s1; sl++)
+                    for (int64_t e0 = 0; e0 < c.Ns; e0 += kRKChunk) {
+                        MFItem it{};
+                        it.type = ITEM_RK;
+                        it.cls = (int16_t)ci;
+                        it.wait_ctr = prev;
+                        it.done_ctr = ctr;
+                        it.R = sl;
+                        it.g0 = (int32_t)e0;
+                        it.W = (int32_t)std::min<int64_t>(c.Ns, e0 + kRKChunk);
+                        items.push_back(it);
+                        count[ctr]++;
+                    }
+            }
+        }
+    }
+    for (auto& it : items) it.wait_need = it.wait_ctr >= 0 ? count[it.wait_ctr] : 0;
+    if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "pencil tile exceeds shared memory");
+    smem_ = smem;
+}
+
+void MFEngine::capture() {
+    cudaStream_t cs = stream_;
+    cudaStream_t own = nullptr;
+    if (cs == nullptr) {  // graphs cannot be captured on the legacy stream
+        CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        cs = own;
+    }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t err = cudaSuccess;
+    for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
+        err = launch_mf_stage(items_d_.as<MFItem>(), nitems_, classes_d_.as<MFClass>(), ctr_d_.as<int>(), nctr_, stage,
+                              (stage - 1) % 2, err_d_.as<int>(), smem_, grid_, cs);
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (own) cudaStreamDestroy(own);
+    if (err != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        throw Error(SGDG_ECUDA, std::string("graph capture: ") + cudaGetErrorString(err != cudaSuccess ? err : e2));
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) {
+        graph_ = nullptr;
+        throw Error(SGDG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+    }
+}
+
+void MFEngine::step(int64_t nsteps) {
+    plan();
+    if (nitems_ == 0 || nsteps <= 0) return;
+    if (!graph_) capture();
+    for (int64_t i = 0; i < nsteps; i++) CK(cudaGraphLaunch(graph_, stream_));
+}
+
+int MFEngine::check_error() {
+    if (!err_d_.p) return SGDG_OK;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, err_d_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (h) {
+        CK(cudaMemsetAsync(err_d_.p, 0, sizeof(int), stream_));
+        return SGDG_ETIMEOUT;
+    }
+    return SGDG_OK;
+}
+
+void MFEngine::get_state(int id, double* host) {
+    plan();
+    const Solve& s = at(id);
+    const ClassArena& c = *classes_[s.cls];
+    CK(cudaMemcpyAsync(host, c.y.as<double>() + (size_t)s.slot * c.Ns, sizeof(double) * c.Ns, cudaMemcpyDeviceToHost,
+                       stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (check_error() != SGDG_OK) throw Error(SGDG_ETIMEOUT, "a bounded device wait gave up; state is unreliable");
+}
+
+void MFEngine::set_state(int id, const double* host) {
+    Solve& s = at(id);
+    if (dirty_ || s.cls < 0) {
+        s.pending.assign(host, host + s.Ns);
+        dirty_ = true;
+        return;
+    }
+    const ClassArena& c = *classes_[s.cls];
+    double* dst = c.y.as<double>() + (size_t)s.slot * c.Ns;
+    CK(cudaMemcpyAsync(dst, host, sizeof(double) * c.Ns, cudaMemcpyHostToDevice, stream_));
+    CK(launch_f64_to_f32(dst, c.u0.as<float>() + (size_t)s.slot * c.Ns, c.Ns, stream_));
+}
+
+void MFEngine::upload_all(const double* host) {
+    plan();
+    int64_t off = 0;
+    for (int id = 0; id < (int)solves_.size(); id++) {
+        const Solve& s = solves_[id];
+        if (!s.live) continue;
+        const ClassArena& c = *classes_[s.cls];
+        CK(cudaMemcpyAsync(c.y.as<double>() + (size_t)s.slot * c.Ns, host + off, sizeof(double) * c.Ns,
+                           cudaMemcpyHostToDevice, stream_));
+        off += s.Ns;
+    }
+    for (auto& cp : classes_)
+        CK(launch_f64_to_f32(cp->y.as<double>(), cp->u0.as<float>(), (int64_t)cp->slots.size() * cp->Ns, stream_));
+}
+
+void MFEngine::download_all(double* host) {
+    plan();
+    int64_t off = 0;
+    int id = 0;
+    const int n = (int)solves_.size();
+    while (id < n) {
+        if (!solves_[id].live) {
+            id++;
+            continue;
+        }
+        // merge a run of ids that sit in consecutive slots of one class
+        const Solve& s = solves_[id];
+        const ClassArena& c = *classes_[s.cls];
+        int run = 1;
+        while (id + run < n && solves_[id + run].live && solves_[id + run].cls == s.cls &&
+               solves_[id + run].slot == s.slot + run)
+            run++;
+        CK(cudaMemcpyAsync(host + off, c.y.as<double>() + (size_t)s.slot * c.Ns, sizeof(double) * c.Ns * run,
+                           cudaMemcpyDeviceToHost, stream_));
+        off += (int64_t)run * c.Ns;
+        id += run;
+    }
+    CK(cudaStreamSynchronize(stream_));
+    if (check_error() != SGDG_OK) throw Error(SGDG_ETIMEOUT, "a bounded device wait gave up; state is unreliable");
+}
+
+void MFEngine::apply(const double* x_dev, double* y_dev) {
+    plan();
+    if (classes_.size() != 1 || classes_[0]->slots.size() != 1) throw Error(SGDG_EINVAL, "apply needs one solve");
+    const ClassArena& c = *classes_[0];
+    CK(launch_f64_to_f32(x_dev, c.u0.as<float>(), c.N, stream_));
+    CK(launch_mf_stage(items_d_.as<MFItem>(), nitems_, classes_d_.as<MFClass>(), ctr_d_.as<int>(), nctr_, 1, 0,
+                       err_d_.as<int>(), smem_, grid_, stream_));
+    CK(launch_f32_to_f64(c.rhs.as<float>(), y_dev, c.N, stream_));
+}
+
+}  // namespace sgdg

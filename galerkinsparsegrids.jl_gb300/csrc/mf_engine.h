@@ -1,0 +1,96 @@
+// mf_engine.h -- host driver of the matrix-free form (batches of solves).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+#include "device_util.h"
+#include "engine.h"
+#include "sgdg_core.h"
+
+namespace sgdg {
+
+struct SolveSpec {
+    int kind = MF_KIND_ADVECT;  // MF_KIND_ADVECT / MF_KIND_WAVE
+    int D = 0, k = 0, n = 0, scheme = 0;
+    double a[8] = {0};          // advection velocity
+    double dt = 0.0;
+    bool apply = false;         // operator application only (no RK): result in rhs
+    int apply_dim = -1;         // apply mode: 0-based dimension, or -1 for the sum over all
+};
+
+class MFEngine {
+   public:
+    explicit MFEngine(cudaStream_t st = nullptr) : stream_(st) {}
+    ~MFEngine();
+    MFEngine(const MFEngine&) = delete;
+    MFEngine& operator=(const MFEngine&) = delete;
+
+    void set_stream(cudaStream_t st);
+    cudaStream_t stream() const { return stream_; }
+
+    // Adds a solve; y0 (host, Ns values) may be null (zero state).
+    int add(const SolveSpec& sp, const double* y0);
+    void remove(int id);
+    void cancel(int id);  // freezes the solve's state (its RK updates are skipped)
+    bool live(int id) const;
+    int64_t state_size(int id) const;
+    int64_t total_size() const;
+
+    void step(int64_t nsteps);                  // RK4 steps of every live solve (async)
+    void get_state(int id, double* host);       // synchronises
+    void set_state(int id, const double* host); // async (pageable memory is staged)
+    void upload_all(const double* host);
+    void download_all(double* host);
+
+    // apply mode (single solve): y_dev = op(x_dev)
+    void apply(const double* x_dev, double* y_dev);
+
+    double dof_updates_per_step() const;
+    int64_t launches_per_step() const { return 4; }
+    int check_error();  // returns SGDG_OK or SGDG_ETIMEOUT after a bounded wait gave up
+
+   private:
+    struct Solve {
+        SolveSpec spec;
+        int64_t N = 0, Ns = 0;
+        int cls = -1, slot = -1;
+        bool live = true, cancelled = false;
+        std::vector<double> pending;  // host state not yet on the device
+    };
+    struct STable {
+        DevBuf rowptr, colblk, val;
+    };
+    struct ClassArena {
+        std::tuple<int, int, int, int, int, bool, int> key;
+        SparseIndex ix;
+        std::vector<std::vector<Pencil>> pencils;  // per dimension
+        std::vector<int32_t> boff_index;           // per (d, pencil): first entry in blockoff
+        int64_t N = 0, Ns = 0;
+        std::vector<int> slots;                    // solve id per slot
+        DevBuf y, acc, u0, u1, rhs, dt, coef, status, blockoff;
+    };
+
+    void plan();
+    void build_items(std::vector<MFItem>& items, int& nctr);
+    const STable& stab(int k, int n);
+    void capture();
+    void drop_graph();
+    Solve& at(int id);
+    const Solve& at(int id) const;
+
+    cudaStream_t stream_ = nullptr;
+    std::vector<Solve> solves_;
+    std::vector<std::unique_ptr<ClassArena>> classes_;
+    std::map<std::pair<int, int>, STable> stabs_;
+    DevBuf classes_d_, items_d_, ctr_d_, err_d_;
+    int nitems_ = 0, nctr_ = 0, grid_ = 0;
+    size_t smem_ = 0;
+    bool dirty_ = true;
+    cudaGraphExec_t graph_ = nullptr;
+};
+
+}  // namespace sgdg
