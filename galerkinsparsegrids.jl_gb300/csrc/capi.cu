@@ -99,7 +99,7 @@ struct sgdg_op {
 };
 
 struct sgdg_batch {
-    MFEngine eng;
+    MFEngine eng;  // its destructor frees device memory only, never touches a stream
     cudaStream_t own = nullptr;
     ~sgdg_batch() {
         if (own) cudaStreamDestroy(own);
@@ -479,8 +479,7 @@ int sgdg_batch_create(sgdg_batch** out) {
 
 int sgdg_batch_destroy(sgdg_batch* b) {
     API_BEGIN
-    if (b) cudaStreamSynchronize(b->eng.stream());
-    delete b;
+    delete b;  // cudaFree of the arenas waits for the batch's outstanding work
     API_END
 }
 

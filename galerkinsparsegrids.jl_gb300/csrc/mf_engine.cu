@@ -24,10 +24,9 @@ cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t
 static constexpr int64_t kGroupReuseBytes = 24LL << 20;  // L2-resident u + rhs per group
 static constexpr int kRKChunk = 8192;
 
-MFEngine::~MFEngine() {
-    if (stream_) cudaStreamSynchronize(stream_);
-    drop_graph();
-}
+// The arenas' cudaFree calls wait for outstanding work; the stream is not
+// touched here because a caller's stream may already be gone.
+MFEngine::~MFEngine() { drop_graph(); }
 
 void MFEngine::set_stream(cudaStream_t st) {
     if (st != stream_) drop_graph();
