@@ -59,11 +59,24 @@ int MFEngine::add(const SolveSpec& sp, const double* y0) {
     dlf1d(sp.k, sp.n);  // validates n >= 2
     s.N = ix.N;
     s.Ns = sp.kind == MF_KIND_WAVE && !sp.apply ? 2 * ix.N : ix.N;
+    // admission: the solve's arena share must fit the HBM budget now
+    const int64_t need = solve_bytes(s.N, s.Ns);
+    const int64_t budget = g_budget.load();
+    if (budget > 0 && g_in_use.load() + pending_bytes_ + need > budget)
+        throw Error(SGDG_ENOMEM_BUDGET, "HBM budget: solve needs " + std::to_string(need) + " bytes, " +
+                                            std::to_string(g_in_use.load() + pending_bytes_) + " of " +
+                                            std::to_string(budget) + " committed");
     if (y0) s.pending.assign(y0, y0 + s.Ns);
     else s.pending.assign(s.Ns, 0.0);
     solves_.push_back(std::move(s));
+    pending_bytes_ += need;
     dirty_ = true;
     return (int)solves_.size() - 1;
+}
+
+int64_t MFEngine::solve_bytes(int64_t N, int64_t Ns) {
+    // y, acc (FP64), two stage inputs (FP32), partial sums (FP32)
+    return Ns * (8 + 8 + 4 + 4) + N * 4;
 }
 
 void MFEngine::remove(int id) {
@@ -151,9 +164,21 @@ void MFEngine::plan() {
         }
         next[f->second]->slots.push_back(id);
     }
-    // 2. arenas, state moves, per-slot tables
+    // 2. arenas, state moves, per-slot tables.  A class's solves only ever
+    // come from the old arena of the same key, which is freed as soon as they
+    // have moved, so the transient overhead is one class arena.
+    std::map<std::tuple<int, int, int, int, int, bool, int>, int> old_of;
+    for (size_t oi = 0; oi < classes_.size(); oi++) old_of[classes_[oi]->key] = (int)oi;
     for (size_t ci = 0; ci < next.size(); ci++) {
         ClassArena& c = *next[ci];
+        auto of = old_of.find(c.key);
+        ClassArena* old_c = of == old_of.end() ? nullptr : classes_[of->second].get();
+        if (old_c) {  // free what the new arena does not need from the old one first
+            old_c->acc.release();
+            old_c->u0.release();
+            old_c->u1.release();
+            old_c->rhs.release();
+        }
         const int ns = (int)c.slots.size();
         if ((int64_t)ns * c.Ns >= (int64_t(1) << 31))
             throw Error(SGDG_EUNSUPPORTED, "a class of solves holds more than 2^31 coefficients");
@@ -198,8 +223,10 @@ void MFEngine::plan() {
         c.coef = upload(coef, stream_);
         c.status = upload(status, stream_);
         CK(launch_f64_to_f32(c.y.as<double>(), c.u0.as<float>(), (int64_t)ns * c.Ns, stream_));
+        if (old_c) old_c->y.release();  // cudaFree waits for the copies above
     }
     CK(cudaStreamSynchronize(stream_));
+    pending_bytes_ = 0;
     // the old arenas are no longer referenced
     classes_.swap(next);
     next.clear();

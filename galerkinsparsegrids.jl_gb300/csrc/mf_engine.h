@@ -52,6 +52,7 @@ class MFEngine {
     double dof_updates_per_step() const;
     int64_t launches_per_step() const { return 4; }
     int check_error();  // returns SGDG_OK or SGDG_ETIMEOUT after a bounded wait gave up
+    static int64_t solve_bytes(int64_t N, int64_t Ns);  // device bytes a solve occupies
 
    private:
     struct Solve {
@@ -88,6 +89,7 @@ class MFEngine {
     std::map<std::pair<int, int>, STable> stabs_;
     DevBuf classes_d_, items_d_, ctr_d_, err_d_;
     int nitems_ = 0, nctr_ = 0, grid_ = 0;
+    int64_t pending_bytes_ = 0;  // admitted but not yet allocated
     size_t smem_ = 0;
     bool dirty_ = true;
     cudaGraphExec_t graph_ = nullptr;
