@@ -263,14 +263,18 @@ __global__ void __launch_bounds__(kMFThreads, 3)
                int in_sel, int* err) {
     extern __shared__ __align__(16) float smem[];
     __shared__ int s_item;
+    __shared__ MFClass s_cls;
     const int tid = threadIdx.x;
     for (;;) {
         if (tid == 0) s_item = atomicAdd(ctr, 1);
         __syncthreads();
         const int ii = s_item;
-        __syncthreads();
         if (ii >= nitems) break;
         const MFItem it = items[ii];
+        // the class descriptor is read many times per item: stage it once
+        constexpr int kClsWords = sizeof(MFClass) / 4;
+        if (tid < kClsWords)
+            reinterpret_cast<int*>(&s_cls)[tid] = reinterpret_cast<const int*>(classes + it.cls)[tid];
         if (it.wait_ctr >= 0) {
             if (tid == 0) {
                 int polls = 0;
@@ -282,9 +286,9 @@ __global__ void __launch_bounds__(kMFThreads, 3)
                     __nanosleep(100);
                 }
             }
-            __syncthreads();
         }
-        const MFClass& C = classes[it.cls];
+        __syncthreads();  // s_cls staged; dependency satisfied
+        const MFClass& C = s_cls;
         if (it.type == ITEM_RK) {
             rk_chunk(it, C, stage, in_sel);
         } else {

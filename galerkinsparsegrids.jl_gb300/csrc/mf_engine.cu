@@ -21,7 +21,7 @@ int mf_columns_per_thread(int k);
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
 
-static constexpr int64_t kGroupReuseBytes = 24LL << 20;  // L2-resident u + rhs per group
+static constexpr int64_t kGroupReuseBytes = 6LL << 20;  // reused u + rhs per group (~4 groups in flight)
 static constexpr int kRKChunk = 8192;
 
 // The arenas' cudaFree calls wait for outstanding work; the stream is not
@@ -290,10 +290,18 @@ void MFEngine::plan() {
     dirty_ = false;
 }
 
+// Work list.  Each class is cut into groups of slots; a group has one phase
+// per dimension pass and (unless applying only) an RK phase, and phase p of a
+// group depends on phase p-1 of the same group.  Groups are emitted in
+// wavefront order -- step t holds phase t-g of group g, oldest group first --
+// so when a phase is handed out, its predecessor was handed out a whole
+// wavefront earlier and is normally complete: CTAs rarely wait, while the
+// groups in flight (about one per phase) keep their reused vectors in L2.
 void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
-    nctr = 1;  // counter 0 hands out items
-    std::vector<int> count;  // items per counter
-    count.push_back(0);
+    struct Group {
+        std::vector<std::vector<MFItem>> phases;
+    };
+    std::vector<Group> groups;
     size_t smem = 64;
     for (size_t ci = 0; ci < classes_.size(); ci++) {
         ClassArena& c = *classes_[ci];
@@ -308,24 +316,24 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
             for (int d = 0; d < D; d++) dims.push_back(d);
         const int ns = (int)c.slots.size();
         const int64_t per_solve = 8 * c.N;
-        const int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
+        const int gs =
+            (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
         int kDm1 = 1;
         for (int q = 0; q < D - 1; q++) kDm1 *= k;
         for (int s0 = 0; s0 < ns; s0 += gs) {
             const int s1 = std::min(ns, s0 + gs);
-            int prev = -1;
+            Group grp;
             for (size_t ph = 0; ph < dims.size(); ph++) {
                 const int d = dims[ph];
                 int kd1 = 1;
                 for (int q = 0; q < d; q++) kd1 *= k;
-                const int ctr = nctr++;
-                count.push_back(0);
+                std::vector<MFItem> list;
                 int bi = 0;
                 for (int dd = 0; dd < d; dd++) bi += (int)c.pencils[dd].size();
                 for (size_t pi = 0; pi < c.pencils[d].size(); pi++) {
                     const Pencil& p = c.pencils[d][pi];
                     const int nrb = 1 << (p.lmax - 1);
-                    const int Wp = cpt * std::max(1, 256 / nrb);
+                    const int Wp = cpt * std::max(1, kMFThreads / nrb);
                     const int64_t cbeg = (int64_t)s0 * p.R, cend = (int64_t)s1 * p.R;
                     const size_t sm = 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * (wave ? 2 : 1));
                     smem = std::max(smem, sm);
@@ -335,8 +343,6 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
                         it.cls = (int16_t)ci;
                         it.d = (int16_t)d;
                         it.flags = (int16_t)((ph == 0 ? TILE_FIRST : 0) | (ph + 1 == dims.size() ? TILE_LAST : 0));
-                        it.wait_ctr = prev;
-                        it.done_ctr = ctr;
                         it.lmax = p.lmax;
                         it.lp = p.lp;
                         it.boff = c.boff_index[bi + pi];
@@ -346,32 +352,46 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
                         it.Wv = (int32_t)std::min<int64_t>(Wp, cend - g0);
                         it.kd1 = kd1;
                         it.kDm1 = kDm1;
-                        items.push_back(it);
-                        count[ctr]++;
+                        list.push_back(it);
                     }
                 }
-                prev = ctr;
+                grp.phases.push_back(std::move(list));
             }
             if (!sp.apply) {
-                const int ctr = nctr++;
-                count.push_back(0);
+                std::vector<MFItem> list;
                 for (int sl = s0; sl < s1; sl++)
                     for (int64_t e0 = 0; e0 < c.Ns; e0 += kRKChunk) {
                         MFItem it{};
                         it.type = ITEM_RK;
                         it.cls = (int16_t)ci;
-                        it.wait_ctr = prev;
-                        it.done_ctr = ctr;
                         it.R = sl;
                         it.g0 = (int32_t)e0;
                         it.W = (int32_t)std::min<int64_t>(c.Ns, e0 + kRKChunk);
-                        items.push_back(it);
-                        count[ctr]++;
+                        list.push_back(it);
                     }
+                grp.phases.push_back(std::move(list));
             }
+            groups.push_back(std::move(grp));
         }
     }
-    for (auto& it : items) it.wait_need = it.wait_ctr >= 0 ? count[it.wait_ctr] : 0;
+    // counters: 0 hands out items; one per (group, phase)
+    nctr = 1;
+    std::vector<std::vector<int>> ctr_of(groups.size());
+    for (size_t g = 0; g < groups.size(); g++)
+        for (size_t p = 0; p < groups[g].phases.size(); p++) ctr_of[g].push_back(nctr++);
+    size_t pmax = 0;
+    for (auto& g : groups) pmax = std::max(pmax, g.phases.size());
+    for (size_t t = 0; t < groups.size() + pmax; t++)
+        for (size_t g = (t >= pmax ? t - pmax + 1 : 0); g <= t && g < groups.size(); g++) {
+            const size_t p = t - g;
+            if (p >= groups[g].phases.size()) continue;
+            for (MFItem it : groups[g].phases[p]) {
+                it.done_ctr = ctr_of[g][p];
+                it.wait_ctr = p > 0 ? ctr_of[g][p - 1] : -1;
+                it.wait_need = p > 0 ? (int32_t)groups[g].phases[p - 1].size() : 0;
+                items.push_back(it);
+            }
+        }
     if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "pencil tile exceeds shared memory");
     smem_ = smem;
 }
