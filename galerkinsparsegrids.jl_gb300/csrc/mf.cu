@@ -65,7 +65,7 @@ __device__ __forceinline__ int elem_off(const int* __restrict__ boff, const Tile
 // blocks of row block rb with cb < nrb; S = hi + lo (two FP32 accumulators).
 template <int K, int CPT>
 __device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict__ src, int W, int nrb, int rb, int jq,
-                                      float (&out)[K][CPT]) {
+                                      int p0, int pstep, float (&out)[K][CPT]) {
     constexpr int RS = ((2 * K + 3) / 4) * 4;
     float2 acc[K][CPT];
 #pragma unroll
@@ -73,7 +73,7 @@ __device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict_
 #pragma unroll
         for (int c = 0; c < CPT; c++) acc[i][c] = make_float2(0.f, 0.f);
     const int pb = __ldg(C.s_rowptr + rb), pe = __ldg(C.s_rowptr + rb + 1);
-    for (int p = pb; p < pe; ++p) {
+    for (int p = pb + p0; p < pe; p += pstep) {
         const int cb = __ldg(C.s_colblk + p);
         if (cb >= nrb) break;
         float x[K][CPT];
@@ -116,6 +116,43 @@ __device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict_
     for (int i = 0; i < K; i++)
 #pragma unroll
         for (int c = 0; c < CPT; c++) out[i][c] = acc[i][c].x + acc[i][c].y;
+}
+
+template <int K, int CPT>
+__device__ __forceinline__ void warp_sum(float (&o)[K][CPT]) {
+#pragma unroll
+    for (int i = 0; i < K; i++)
+#pragma unroll
+        for (int c = 0; c < CPT; c++)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) o[i][c] += __shfl_xor_sync(0xffffffffu, o[i][c], off);
+}
+
+// Applies the pencil's 1D operator to src for every (row block, column quad)
+// of the tile and hands each result to emit(rb, jq, out).  In the
+// hierarchical basis a coarse row block couples to most blocks of the pencil
+// (row block 0 to all of them) while a fine one couples to O(levels), so the
+// coarse rows (rb < rlong) are shared by a warp -- lanes split the block list,
+// a fixed shuffle tree sums -- and the fine rows get one thread each.
+template <int K, int CPT, class Emit>
+__device__ __forceinline__ void apply_rows(const MFClass& C, const float* __restrict__ src, int W, int nrb, int lwq,
+                                           int rlong, Emit&& emit) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nql = rlong << lwq;
+    for (int u = warp; u < nql; u += kMFThreads / 32) {
+        const int rb = u >> lwq, jq = u & ((1 << lwq) - 1);
+        float o[K][CPT];
+        sweep<K, CPT>(C, src, W, nrb, rb, jq, lane, 32, o);
+        warp_sum<K, CPT>(o);
+        if (lane == 0) emit(rb, jq, o);
+    }
+    const int nq = nrb << lwq;
+    for (int q = nql + (int)threadIdx.x; q < nq; q += kMFThreads) {
+        const int rb = q >> lwq, jq = q & ((1 << lwq) - 1);
+        float o[K][CPT];
+        sweep<K, CPT>(C, src, W, nrb, rb, jq, 0, 1, o);
+        emit(rb, jq, o);
+    }
 }
 
 template <int K, int CPT, bool WAVE>
@@ -167,12 +204,9 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
     cp_async_wait_all();
     __syncthreads();
     const int lwq = lw - (CPT == 4 ? 2 : 1);
-    const int nq = nrb << lwq;
+    const int rlong = it.lmax > 4 ? 1 << (it.lmax - 5) : 0;  // row blocks of levels <= lmax - 4
     if (WAVE) {
-        for (int q = tid; q < nq; q += kMFThreads) {
-            const int rb = q >> lwq, jq = q & ((1 << lwq) - 1);
-            float o[K][CPT];
-            sweep<K, CPT>(C, X, W, nrb, rb, jq, o);
+        apply_rows<K, CPT>(C, X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) {
 #pragma unroll
             for (int i = 0; i < K; i++) {
                 float* yp = Y + (rb * K + i) * W + jq * CPT;
@@ -181,14 +215,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
                 else
                     *reinterpret_cast<float2*>(yp) = make_float2(o[i][0], o[i][1]);
             }
-        }
+        });
         __syncthreads();
     }
     const bool first = (it.flags & TILE_FIRST) != 0;
-    for (int q = tid; q < nq; q += kMFThreads) {
-        const int rb = q >> lwq, jq = q & ((1 << lwq) - 1);
-        float o[K][CPT];
-        sweep<K, CPT>(C, WAVE ? Y : X, W, nrb, rb, jq, o);
+    apply_rows<K, CPT>(C, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) {
         // element offsets of the quad in the rhs arena (-1: padding column)
         int off[K][CPT];
 #pragma unroll
@@ -215,7 +246,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
 #pragma unroll
             for (int i = 0; i < K; i++)
                 if (off[i][c] >= 0) __stcg(C.rhs + off[i][c], o[i][c]);
-    }
+    });
 }
 
 __device__ void rk_chunk(const MFItem& it, const MFClass& C, int stage, int in_sel) {
