@@ -92,6 +92,21 @@ int sgdg_apply(sgdg_op *op, int which, int method, const double *x, double *y);
 /* Same with device pointers on a caller stream (cudaStream_t, may be NULL). */
 int sgdg_apply_device(sgdg_op *op, int which, int method, const double *x_dev, double *y_dev, void *stream);
 
+/* Matrix-free FP32 y = D_d x (which = 1..D) or y = laplacian x (which = 0) for
+ * (D, k, n, scheme), device pointers, without allocating any device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- code whose device memory is owned by another allocator (a
+ * framework's caching or stream-ordered pool), runtimes that forbid device
+ * allocation after start-up, and latency-critical loops that cannot take
+ * cudaMalloc/cudaFree's implicit device synchronisation.  All scratch lives
+ * in one 16 MiB device array that every GPU loading the library holds until
+ * exit; problems needing more are rejected with SGDG_EINVAL.  Calls share
+ * that array: calls overlapping on the GPU race and must be serialised.  The
+ * first call on a device resolves the array's address; make it before any
+ * stream capture.  Synchronous on `stream` (cudaStream_t, may be NULL). */
+int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, const double *x_dev, double *y_dev,
+                       void *stream);
+
 /* ---- evolvers ----------------------------------------------------------- */
 /* wave_evolve (src/pdes.jl:54-70) with classical RK4 and nsteps fixed steps on
  * [t0, t1]: u_tt = laplacian(u), state [f; v].  Writes nout >= 2 equally
