@@ -62,7 +62,7 @@ struct MFItem {
     int32_t kDm1;      // pass: k^(D-1)
 };
 
-constexpr int kMFThreads = 256;
+constexpr int kMFThreads = 128;
 constexpr int kSpinLimit = 1 << 22;  // polls of a dependency counter before giving up
 
 }  // namespace sgdg

@@ -155,8 +155,21 @@ __device__ __forceinline__ void apply_rows(const MFClass& C, const float* __rest
     }
 }
 
+// Waits (thread 0, bounded) until counter ctr reaches need; the caller's
+// following __syncthreads publishes the outcome to the CTA.
+__device__ __forceinline__ void wait_counter(const int* ctr, int need, int* err) {
+    int polls = 0;
+    while (ld_acquire(ctr) < need) {
+        if (++polls > kSpinLimit || ld_relaxed(err) != 0) {
+            atomicExch(err, 1);
+            break;
+        }
+        __nanosleep(100);
+    }
+}
+
 template <int K, int CPT, bool WAVE>
-__device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float* smem) {
+__device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float* smem, const int* ctr, int* err) {
     const int tid = threadIdx.x;
     const int nrb = 1 << (it.lmax - 1);
     const int m = nrb * K;
@@ -168,6 +181,8 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
     float* X = reinterpret_cast<float*>(cb + W);  // 12W bytes in: 16-aligned for W % 4 == 0, 8 for W % 2 == 0
     float* Y = X + m * W;
     const int kD = C.kD, kd1 = it.kd1, lp = it.lp, R = it.R, kDm1 = it.kDm1;
+    __shared__ int sboff[32];
+    if (tid < it.lmax) sboff[tid] = (int)C.blockoff[it.boff + tid];  // level-block offsets (N < 2^31)
     for (int j = tid; j < W; j += kMFThreads) {
         if (j < Wv) {
             const int g = it.g0 + j;
@@ -184,11 +199,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
     }
     __syncthreads();
     const TileCols cols{cslot, ca, cb};
-    const int64_t* __restrict__ pboff = C.blockoff + it.boff;
-    // level-block offsets of the pencil fit in int (N < 2^31)
-    __shared__ int sboff[32];
-    if (tid < it.lmax) sboff[tid] = (int)pboff[tid];
-    __syncthreads();
+    // gather the stage input (written by the previous launch) into X
     const float* __restrict__ uin = C.u[in_sel];
     const int ne = m << lw;
     for (int e = tid; e < ne; e += kMFThreads) {
@@ -205,48 +216,39 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
     __syncthreads();
     const int lwq = lw - (CPT == 4 ? 2 : 1);
     const int rlong = it.lmax > 4 ? 1 << (it.lmax - 5) : 0;  // row blocks of levels <= lmax - 4
+    auto store = [&](float* dst, int rb, int jq, float(&o)[K][CPT]) {
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            float* yp = dst + (rb * K + i) * W + jq * CPT;
+            if constexpr (CPT == 4)
+                *reinterpret_cast<float4*>(yp) = make_float4(o[i][0], o[i][1], o[i][2], o[i][3]);
+            else
+                *reinterpret_cast<float2*>(yp) = make_float2(o[i][0], o[i][1]);
+        }
+    };
+    // result Z of the tile: wave X -> Y -> X (X is dead after the first
+    // sweep), advection X -> Y
+    float* Z = Y;
     if (WAVE) {
-        apply_rows<K, CPT>(C, X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) {
-#pragma unroll
-            for (int i = 0; i < K; i++) {
-                float* yp = Y + (rb * K + i) * W + jq * CPT;
-                if constexpr (CPT == 4)
-                    *reinterpret_cast<float4*>(yp) = make_float4(o[i][0], o[i][1], o[i][2], o[i][3]);
-                else
-                    *reinterpret_cast<float2*>(yp) = make_float2(o[i][0], o[i][1]);
-            }
-        });
+        apply_rows<K, CPT>(C, X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Y, rb, jq, o); });
         __syncthreads();
+        Z = X;
     }
+    apply_rows<K, CPT>(C, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Z, rb, jq, o); });
+    // the partial sums of this group's previous pass must be complete
+    if (it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
+    __syncthreads();
     const bool first = (it.flags & TILE_FIRST) != 0;
-    apply_rows<K, CPT>(C, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) {
-        // element offsets of the quad in the rhs arena (-1: padding column)
-        int off[K][CPT];
-#pragma unroll
-        for (int c = 0; c < CPT; c++) {
-            const int j = jq * CPT + c;
-            const int s = cslot[j];
-            const float coef = s >= 0 ? __ldg(C.coef + s * 8 + it.d) : 0.f;
-            const int e0 = s >= 0 ? s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, 0, j) : -1;
-#pragma unroll
-            for (int i = 0; i < K; i++) {
-                off[i][c] = e0 < 0 ? -1 : e0 + i * kd1;
-                o[i][c] *= coef;
-            }
-        }
-        if (!first) {
-#pragma unroll
-            for (int c = 0; c < CPT; c++)
-#pragma unroll
-                for (int i = 0; i < K; i++)
-                    if (off[i][c] >= 0) o[i][c] += __ldcg(C.rhs + off[i][c]);
-        }
-#pragma unroll
-        for (int c = 0; c < CPT; c++)
-#pragma unroll
-            for (int i = 0; i < K; i++)
-                if (off[i][c] >= 0) __stcg(C.rhs + off[i][c], o[i][c]);
-    });
+    for (int e = tid; e < ne; e += kMFThreads) {
+        const int row = e >> lw, j = e & (W - 1);
+        const int s = cslot[j];
+        if (s < 0) continue;
+        const int rb = row / K, i = row - rb * K;
+        float* rp = C.rhs + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
+        float v = __ldg(C.coef + s * 8 + it.d) * Z[e];
+        if (!first) v += __ldcg(rp);
+        __stcg(rp, v);
+    }
 }
 
 __device__ void rk_chunk(const MFItem& it, const MFClass& C, int stage, int in_sel) {
@@ -289,51 +291,51 @@ __device__ void rk_chunk(const MFItem& it, const MFClass& C, int stage, int in_s
     }
 }
 
-__global__ void __launch_bounds__(kMFThreads, 3)
+__global__ void __launch_bounds__(kMFThreads, 6)
     k_mf_stage(const MFItem* __restrict__ items, int nitems, const MFClass* __restrict__ classes, int* ctr, int stage,
                int in_sel, int* err) {
     extern __shared__ __align__(16) float smem[];
     __shared__ int s_item;
+    __shared__ MFItem s_it;
     __shared__ MFClass s_cls;
     const int tid = threadIdx.x;
+    constexpr int kItemWords = sizeof(MFItem) / 4;
+    constexpr int kClsWords = sizeof(MFClass) / 4;
+    static_assert(kItemWords <= 32, "item fits one warp");
     for (;;) {
-        if (tid == 0) s_item = atomicAdd(ctr, 1);
-        __syncthreads();
-        const int ii = s_item;
-        if (ii >= nitems) break;
-        const MFItem it = items[ii];
-        // the class descriptor is read many times per item: stage it once
-        constexpr int kClsWords = sizeof(MFClass) / 4;
-        if (tid < kClsWords)
-            reinterpret_cast<int*>(&s_cls)[tid] = reinterpret_cast<const int*>(classes + it.cls)[tid];
-        if (it.wait_ctr >= 0) {
-            if (tid == 0) {
-                int polls = 0;
-                while (ld_acquire(ctr + it.wait_ctr) < it.wait_need) {
-                    if (++polls > kSpinLimit || ld_relaxed(err) != 0) {
-                        atomicExch(err, 1);
-                        break;
-                    }
-                    __nanosleep(100);
-                }
+        // warp 0 takes the next item and stages it and its class descriptor
+        if (tid < 32) {
+            int ii = 0;
+            if (tid == 0) ii = atomicAdd(ctr, 1);
+            ii = __shfl_sync(0xffffffffu, ii, 0);
+            if (ii < nitems) {
+                if (tid < kItemWords) reinterpret_cast<int*>(&s_it)[tid] = reinterpret_cast<const int*>(items + ii)[tid];
+                const int cls = items[ii].cls;
+                for (int w = tid; w < kClsWords; w += 32)
+                    reinterpret_cast<int*>(&s_cls)[w] = reinterpret_cast<const int*>(classes + cls)[w];
             }
+            if (tid == 0) s_item = ii;
         }
-        __syncthreads();  // s_cls staged; dependency satisfied
+        __syncthreads();
+        if (s_item >= nitems) break;
+        const MFItem& it = s_it;
         const MFClass& C = s_cls;
         if (it.type == ITEM_RK) {
+            if (it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
+            __syncthreads();
             rk_chunk(it, C, stage, in_sel);
         } else {
             switch (C.k * 2 + C.kind) {
-                case 2: pass_tile<1, 4, false>(it, C, in_sel, smem); break;
-                case 3: pass_tile<1, 4, true>(it, C, in_sel, smem); break;
-                case 4: pass_tile<2, 4, false>(it, C, in_sel, smem); break;
-                case 5: pass_tile<2, 4, true>(it, C, in_sel, smem); break;
-                case 6: pass_tile<3, 4, false>(it, C, in_sel, smem); break;
-                case 7: pass_tile<3, 4, true>(it, C, in_sel, smem); break;
-                case 8: pass_tile<4, 2, false>(it, C, in_sel, smem); break;
-                case 9: pass_tile<4, 2, true>(it, C, in_sel, smem); break;
-                case 10: pass_tile<5, 2, false>(it, C, in_sel, smem); break;
-                case 11: pass_tile<5, 2, true>(it, C, in_sel, smem); break;
+                case 2: pass_tile<1, 4, false>(it, C, in_sel, smem, ctr, err); break;
+                case 3: pass_tile<1, 4, true>(it, C, in_sel, smem, ctr, err); break;
+                case 4: pass_tile<2, 4, false>(it, C, in_sel, smem, ctr, err); break;
+                case 5: pass_tile<2, 4, true>(it, C, in_sel, smem, ctr, err); break;
+                case 6: pass_tile<3, 4, false>(it, C, in_sel, smem, ctr, err); break;
+                case 7: pass_tile<3, 4, true>(it, C, in_sel, smem, ctr, err); break;
+                case 8: pass_tile<4, 2, false>(it, C, in_sel, smem, ctr, err); break;
+                case 9: pass_tile<4, 2, true>(it, C, in_sel, smem, ctr, err); break;
+                case 10: pass_tile<5, 2, false>(it, C, in_sel, smem, ctr, err); break;
+                case 11: pass_tile<5, 2, true>(it, C, in_sel, smem, ctr, err); break;
                 default: break;
             }
         }

@@ -335,7 +335,7 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
                     const int nrb = 1 << (p.lmax - 1);
                     const int Wp = cpt * std::max(1, kMFThreads / nrb);
                     const int64_t cbeg = (int64_t)s0 * p.R, cend = (int64_t)s1 * p.R;
-                    const size_t sm = 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * (wave ? 2 : 1));
+                    const size_t sm = 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * 2);
                     smem = std::max(smem, sm);
                     for (int64_t g0 = cbeg; g0 < cend; g0 += Wp) {
                         MFItem it{};

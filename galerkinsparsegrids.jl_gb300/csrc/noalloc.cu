@@ -148,7 +148,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                 for (auto o : p.blockoff) boff.push_back(o);
                 const int nrb = 1 << (p.lmax - 1);
                 const int Wp = cpt * std::max(1, kMFThreads / nrb);
-                smem = std::max(smem, 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * (wave ? 2 : 1)));
+                smem = std::max(smem, 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * 2));
                 for (int64_t g0 = 0; g0 < p.R; g0 += Wp) {
                     MFItem it{};
                     it.type = ITEM_PASS;
