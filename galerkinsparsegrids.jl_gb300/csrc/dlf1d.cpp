@@ -90,7 +90,6 @@ static DLF1D build_dlf(int k, int n) {
         double r0, r1;
         block_support(op.blk_level[rb], op.blk_cell[rb], r0, r1);
         const auto& row = fns[rb];
-        // jump points of the row functions
         // jump points of the row functions, taken mod 1 (0 and 1 are one point)
         std::vector<double> E;
         if (row[0].level == 0)
@@ -156,6 +155,42 @@ std::shared_ptr<const DLF1D> dlf1d(int k, int n) {
     std::lock_guard<std::mutex> g(mu);
     cache[{k, n}] = op;
     return op;
+}
+
+}  // namespace sgdg
+
+namespace sgdg {
+
+MFOperator mf_operator(int k, int n) {
+    auto op = dlf1d(k, n);
+    MFOperator M;
+    M.k = k;
+    M.n = n;
+    M.rs = ((2 * k + 3) / 4) * 4;
+    double vmax = 0.0;
+    for (double v : op->val) vmax = std::max(vmax, std::fabs(v));
+    const double drop = 1e-10 * vmax;
+    M.rowptr.assign(op->nblocks + 1, 0);
+    for (int rb = 0; rb < op->nblocks; rb++) {
+        for (int p = op->rowptr[rb]; p < op->rowptr[rb + 1]; p++) {
+            const double* b = &op->val[(size_t)p * k * k];
+            double bmax = 0.0;
+            for (int t = 0; t < k * k; t++) bmax = std::max(bmax, std::fabs(b[t]));
+            if (bmax <= drop) continue;
+            M.colblk.push_back(op->colblk[p]);
+            const size_t base = M.val.size();
+            M.val.resize(base + (size_t)k * M.rs, 0.f);
+            for (int i = 0; i < k; i++)
+                for (int j = 0; j < k; j++) {
+                    const double x = b[i * k + j];
+                    const float hi = (float)x;
+                    M.val[base + (size_t)i * M.rs + 2 * j] = hi;
+                    M.val[base + (size_t)i * M.rs + 2 * j + 1] = (float)(x - (double)hi);
+                }
+        }
+        M.rowptr[rb + 1] = (int32_t)M.colblk.size();
+    }
+    return M;
 }
 
 }  // namespace sgdg

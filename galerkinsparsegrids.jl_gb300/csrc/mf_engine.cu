@@ -115,24 +115,11 @@ const MFEngine::STable& MFEngine::stab(int k, int n) {
     auto key = std::make_pair(k, n);
     auto it = stabs_.find(key);
     if (it != stabs_.end()) return it->second;
-    auto op = dlf1d(k, n);
-    // per block: k rows of (hi, lo) pairs, each row padded to rs floats
-    const int rs = ((2 * k + 3) / 4) * 4;
-    const size_t nb = op->colblk.size();
-    std::vector<float> v(nb * k * rs, 0.f);
-    for (size_t b = 0; b < nb; b++)
-        for (int i = 0; i < k; i++)
-            for (int j = 0; j < k; j++) {
-                const double x = op->val[b * k * k + i * k + j];
-                const float hi = (float)x;
-                const float lo = (float)(x - (double)hi);
-                v[(b * k + i) * rs + 2 * j] = hi;
-                v[(b * k + i) * rs + 2 * j + 1] = lo;
-            }
+    const MFOperator M = mf_operator(k, n);
     STable S;
-    S.rowptr = upload(op->rowptr, stream_);
-    S.colblk = upload(op->colblk, stream_);
-    S.val = upload(v, stream_);
+    S.rowptr = upload(M.rowptr, stream_);
+    S.colblk = upload(M.colblk, stream_);
+    S.val = upload(M.val, stream_);
     CK(cudaStreamSynchronize(stream_));
     return stabs_.emplace(key, std::move(S)).first->second;
 }

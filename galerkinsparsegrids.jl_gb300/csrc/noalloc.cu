@@ -111,21 +111,13 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         }
         cudaStream_t st = (cudaStream_t)stream;
         const bool wave = which == SGDG_OP_LAPLACIAN;
-        const auto op = dlf1d(k, n);
         const int N = (int)ix.N;
 
-        // 1D operator as FP32 hi + lo pairs, rows padded to rs floats
-        const int rs = ((2 * k + 3) / 4) * 4;
-        const size_t nb = op->colblk.size();
-        std::vector<float> sval(nb * k * rs, 0.f);
-        for (size_t b = 0; b < nb; b++)
-            for (int i = 0; i < k; i++)
-                for (int j = 0; j < k; j++) {
-                    const double v = op->val[b * k * k + i * k + j];
-                    const float hi = (float)v;
-                    sval[(b * k + i) * rs + 2 * j] = hi;
-                    sval[(b * k + i) * rs + 2 * j + 1] = (float)(v - (double)hi);
-                }
+        // 1D operator blocks as the matrix-free kernel applies them
+        const MFOperator M = mf_operator(k, n);
+        const MFOperator* op = &M;
+        const int rs = M.rs;
+        const std::vector<float>& sval = M.val;
 
         // pencil tiles of the requested dimensions: one phase per dimension
         std::vector<int> dims;

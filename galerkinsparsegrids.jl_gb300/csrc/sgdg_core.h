@@ -64,6 +64,22 @@ struct DLF1D {
 };
 std::shared_ptr<const DLF1D> dlf1d(int k, int n);
 
+// The 1D operator as the matrix-free kernels apply it: block CSR over the
+// blocks that are not zero up to roundoff, each entry as an FP32 (hi, lo)
+// pair, rows padded to rs floats.  A wavelet with k vanishing moments is
+// orthogonal to the derivative of anything polynomial on its support, so a
+// fine/coarse block pair vanishes unless the fine support touches a break of
+// the coarse function; the reference's structural pattern keeps such blocks
+// as numerical zeros (the plain CSR form keeps them too).  Blocks are dropped
+// when their largest entry is below 1e-10 of the operator's largest entry;
+// zero blocks sit below 1e-13 and kept ones above 1e-3 of it.
+struct MFOperator {
+    int k = 0, n = 0, rs = 0;
+    std::vector<int32_t> rowptr, colblk;
+    std::vector<float> val;
+};
+MFOperator mf_operator(int k, int n);
+
 // ------------------------------------------------------------ index map ----
 // Sparse-grid coefficient layout of src/dg_vmethods.jl:246-286: level tuples
 // in Julia CartesianIndices order (dimension 1 fastest), then cells, then modes.

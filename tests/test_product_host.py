@@ -162,3 +162,19 @@ def test_compute_without_gpu_fails_loudly(sgdg):
     with pytest.raises(sgdg.SGDGError) as e:
         op.apply(np.zeros(op.N), 1)
     assert e.value.code == 6  # SGDG_ENOGPU: no CPU fallback
+
+
+@pytest.mark.parametrize("k,n", [(1, 5), (2, 8), (3, 7), (4, 6), (5, 6), (3, 2)])
+def test_zero_blocks_are_separated_from_genuine_ones(sgdg, k, n):
+    # The matrix-free form skips the k x k blocks whose largest entry is below
+    # 1e-10 of the operator's largest: those vanish mathematically (vanishing
+    # moments of the finer wavelet) and sit at roundoff, far from every genuine
+    # block.
+    A = sgdg.periodic_DLF_matrix(k, n).tocoo()
+    mx = np.abs(A.data).max()
+    bm = {}
+    for r, c, v in zip(A.row // k, A.col // k, np.abs(A.data)):
+        bm[(r, c)] = max(bm.get((r, c), 0.0), v)
+    rel = np.array(list(bm.values())) / mx
+    assert not np.any((rel > 1e-12) & (rel < 1e-4))
+    assert np.sum(rel > 1e-10) < len(rel) or n <= 2
