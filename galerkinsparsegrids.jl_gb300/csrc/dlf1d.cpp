@@ -170,6 +170,9 @@ MFOperator mf_operator(int k, int n) {
     double vmax = 0.0;
     for (double v : op->val) vmax = std::max(vmax, std::fabs(v));
     const double drop = 1e-10 * vmax;
+    // blocks equal to 1e-12 of vmax share one table entry (they are the same
+    // block up to the roundoff of their separate evaluation)
+    std::map<std::vector<long long>, int> ids;
     M.rowptr.assign(op->nblocks + 1, 0);
     for (int rb = 0; rb < op->nblocks; rb++) {
         for (int p = op->rowptr[rb]; p < op->rowptr[rb + 1]; p++) {
@@ -177,18 +180,30 @@ MFOperator mf_operator(int k, int n) {
             double bmax = 0.0;
             for (int t = 0; t < k * k; t++) bmax = std::max(bmax, std::fabs(b[t]));
             if (bmax <= drop) continue;
-            M.colblk.push_back(op->colblk[p]);
-            const size_t base = M.val.size();
-            M.val.resize(base + (size_t)k * M.rs, 0.f);
-            for (int i = 0; i < k; i++)
-                for (int j = 0; j < k; j++) {
-                    const double x = b[i * k + j];
-                    const float hi = (float)x;
-                    M.val[base + (size_t)i * M.rs + 2 * j] = hi;
-                    M.val[base + (size_t)i * M.rs + 2 * j + 1] = (float)(x - (double)hi);
-                }
+            std::vector<long long> key(k * k);
+            for (int t = 0; t < k * k; t++) key[t] = std::llround(b[t] / vmax * 1e12);
+            auto it = ids.find(key);
+            int id;
+            if (it == ids.end()) {
+                id = M.ndist++;
+                ids.emplace(std::move(key), id);
+                const size_t base = M.val.size();
+                M.val.resize(base + (size_t)k * M.rs, 0.f);
+                for (int i = 0; i < k; i++)
+                    for (int j = 0; j < k; j++) {
+                        const double x = b[i * k + j];
+                        const float hi = (float)x;
+                        M.val[base + (size_t)i * M.rs + 2 * j] = hi;
+                        M.val[base + (size_t)i * M.rs + 2 * j + 1] = (float)(x - (double)hi);
+                    }
+            } else {
+                id = it->second;
+            }
+            if (id >= 4096 || op->colblk[p] >= (1 << 19))
+                throw Error(7, "1D operator too large for the matrix-free block table");
+            M.ent.push_back((op->colblk[p] << 12) | id);
         }
-        M.rowptr[rb + 1] = (int32_t)M.colblk.size();
+        M.rowptr[rb + 1] = (int32_t)M.ent.size();
     }
     return M;
 }

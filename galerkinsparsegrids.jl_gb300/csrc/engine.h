@@ -28,9 +28,9 @@ enum : int { TILE_FIRST = 1, TILE_LAST = 2 };
 enum : int { ITEM_PASS = 0, ITEM_RK = 1 };
 
 struct MFClass {
-    const int32_t* s_rowptr;  // 1D operator, block CSR over 2^n row blocks
-    const int32_t* s_colblk;
-    const float* s_val;       // per block: k rows of (hi, lo) pairs, each row padded to rs floats
+    const int32_t* s_rowptr;  // 1D operator, block CSR over 2^n row blocks (2^n + 1 entries)
+    const int32_t* s_ent;     // per stored block: column block << 12 | distinct block id
+    const float* s_val;       // distinct blocks: k rows of (hi, lo) pairs, each row padded to rs floats
     const int64_t* blockoff;  // level-block offsets of every pencil of the class
     double* y;                // arenas, nslots * Ns
     double* acc;
@@ -41,7 +41,17 @@ struct MFClass {
     const int32_t* status;    // per slot, nonzero = skip the RK update
     int32_t N, Ns;
     int32_t D, k, kD, kind, rs;
+    int32_t s_nrow, s_nent, s_nval;  // table sizes (ints, ints, floats) for the shared-memory copy
+    int32_t s_shared;                // 1: pass tiles read a shared-memory copy of the table; 0: global memory
 };
+
+// bytes of the shared-memory copy of a class's 1D operator table
+inline int mf_table_bytes(int nrow, int nent, int nval) {
+    return (((nrow + nent) * 4 + 15) / 16) * 16 + nval * 4;
+}
+// tables above this size are read from global memory (their row lists grow
+// like 2^n n; the distinct blocks stay a few hundred)
+constexpr int kMFTableSmemMax = 48 * 1024;
 
 struct MFItem {
     int16_t type;      // ITEM_PASS / ITEM_RK

@@ -63,8 +63,14 @@ __device__ __forceinline__ int elem_off(const int* __restrict__ boff, const Tile
 
 // acc[i][c] += S(rb, cb)[i][jj] * src[cb*K + jj][jq*CPT + c] over the stored
 // blocks of row block rb with cb < nrb; S = hi + lo (two FP32 accumulators).
+struct OpTable {  // shared-memory copy of the class's 1D operator table
+    const int* rowptr;
+    const int* ent;
+    const float* val;
+};
+
 template <int K, int CPT>
-__device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict__ src, int W, int nrb, int rb, int jq,
+__device__ __forceinline__ void sweep(const OpTable& T, const float* __restrict__ src, int W, int nrb, int rb, int jq,
                                       int p0, int pstep, float (&out)[K][CPT]) {
     constexpr int RS = ((2 * K + 3) / 4) * 4;
     float2 acc[K][CPT];
@@ -72,9 +78,10 @@ __device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict_
     for (int i = 0; i < K; i++)
 #pragma unroll
         for (int c = 0; c < CPT; c++) acc[i][c] = make_float2(0.f, 0.f);
-    const int pb = __ldg(C.s_rowptr + rb), pe = __ldg(C.s_rowptr + rb + 1);
+    const int pb = T.rowptr[rb], pe = T.rowptr[rb + 1];
     for (int p = pb + p0; p < pe; p += pstep) {
-        const int cb = __ldg(C.s_colblk + p);
+        const int e = T.ent[p];
+        const int cb = e >> 12;
         if (cb >= nrb) break;
         float x[K][CPT];
 #pragma unroll
@@ -92,13 +99,13 @@ __device__ __forceinline__ void sweep(const MFClass& C, const float* __restrict_
                 x[jj][1] = v.y;
             }
         }
-        const float4* sv = reinterpret_cast<const float4*>(C.s_val + (size_t)p * (K * RS));
+        const float4* sv = reinterpret_cast<const float4*>(T.val + (e & 4095) * (K * RS));
 #pragma unroll
         for (int i = 0; i < K; i++) {
             float srow[RS];
 #pragma unroll
             for (int v = 0; v < RS / 4; v++) {
-                const float4 f = __ldg(sv + i * (RS / 4) + v);
+                const float4 f = sv[i * (RS / 4) + v];
                 srow[4 * v] = f.x;
                 srow[4 * v + 1] = f.y;
                 srow[4 * v + 2] = f.z;
@@ -135,14 +142,14 @@ __device__ __forceinline__ void warp_sum(float (&o)[K][CPT]) {
 // coarse rows (rb < rlong) are shared by a warp -- lanes split the block list,
 // a fixed shuffle tree sums -- and the fine rows get one thread each.
 template <int K, int CPT, class Emit>
-__device__ __forceinline__ void apply_rows(const MFClass& C, const float* __restrict__ src, int W, int nrb, int lwq,
+__device__ __forceinline__ void apply_rows(const OpTable& T, const float* __restrict__ src, int W, int nrb, int lwq,
                                            int rlong, Emit&& emit) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nql = rlong << lwq;
     for (int u = warp; u < nql; u += kMFThreads / 32) {
         const int rb = u >> lwq, jq = u & ((1 << lwq) - 1);
         float o[K][CPT];
-        sweep<K, CPT>(C, src, W, nrb, rb, jq, lane, 32, o);
+        sweep<K, CPT>(T, src, W, nrb, rb, jq, lane, 32, o);
         warp_sum<K, CPT>(o);
         if (lane == 0) emit(rb, jq, o);
     }
@@ -150,7 +157,7 @@ __device__ __forceinline__ void apply_rows(const MFClass& C, const float* __rest
     for (int q = nql + (int)threadIdx.x; q < nq; q += kMFThreads) {
         const int rb = q >> lwq, jq = q & ((1 << lwq) - 1);
         float o[K][CPT];
-        sweep<K, CPT>(C, src, W, nrb, rb, jq, 0, 1, o);
+        sweep<K, CPT>(T, src, W, nrb, rb, jq, 0, 1, o);
         emit(rb, jq, o);
     }
 }
@@ -169,7 +176,8 @@ __device__ __forceinline__ void wait_counter(const int* ctr, int need, int* err)
 }
 
 template <int K, int CPT, bool WAVE>
-__device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float* smem, const int* ctr, int* err) {
+__device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int in_sel, float* smem, const int* ctr,
+                          int* err) {
     const int tid = threadIdx.x;
     const int nrb = 1 << (it.lmax - 1);
     const int m = nrb * K;
@@ -230,11 +238,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, int in_sel, float*
     // sweep), advection X -> Y
     float* Z = Y;
     if (WAVE) {
-        apply_rows<K, CPT>(C, X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Y, rb, jq, o); });
+        apply_rows<K, CPT>(T, X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Y, rb, jq, o); });
         __syncthreads();
         Z = X;
     }
-    apply_rows<K, CPT>(C, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Z, rb, jq, o); });
+    apply_rows<K, CPT>(T, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Z, rb, jq, o); });
     // the partial sums of this group's previous pass must be complete
     if (it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
@@ -293,15 +301,19 @@ __device__ void rk_chunk(const MFItem& it, const MFClass& C, int stage, int in_s
 
 __global__ void __launch_bounds__(kMFThreads, 6)
     k_mf_stage(const MFItem* __restrict__ items, int nitems, const MFClass* __restrict__ classes, int* ctr, int stage,
-               int in_sel, int* err) {
+               int in_sel, int* err, int table_bytes) {
+    // dynamic shared memory: [1D operator table of the current class][tile]
     extern __shared__ __align__(16) float smem[];
+    float* tile = smem + table_bytes / 4;
     __shared__ int s_item;
+    __shared__ int s_cached;  // class whose table is in shared memory (-1: none)
     __shared__ MFItem s_it;
     __shared__ MFClass s_cls;
     const int tid = threadIdx.x;
     constexpr int kItemWords = sizeof(MFItem) / 4;
     constexpr int kClsWords = sizeof(MFClass) / 4;
     static_assert(kItemWords <= 32, "item fits one warp");
+    if (tid == 0) s_cached = -1;
     for (;;) {
         // warp 0 takes the next item and stages it and its class descriptor
         if (tid < 32) {
@@ -325,17 +337,32 @@ __global__ void __launch_bounds__(kMFThreads, 6)
             __syncthreads();
             rk_chunk(it, C, stage, in_sel);
         } else {
+            OpTable T{C.s_rowptr, C.s_ent, C.s_val};
+            if (C.s_shared) {
+                int* trow = reinterpret_cast<int*>(smem);
+                int* tent = trow + C.s_nrow;
+                float* tval = smem + (((C.s_nrow + C.s_nent) * 4 + 15) / 16) * 4;
+                if (s_cached != it.cls) {  // copy the class's operator table (uniform branch)
+                    for (int i = tid; i < C.s_nrow; i += kMFThreads) trow[i] = C.s_rowptr[i];
+                    for (int i = tid; i < C.s_nent; i += kMFThreads) tent[i] = C.s_ent[i];
+                    for (int i = tid; i < C.s_nval / 4; i += kMFThreads)
+                        reinterpret_cast<float4*>(tval)[i] = reinterpret_cast<const float4*>(C.s_val)[i];
+                    __syncthreads();
+                    if (tid == 0) s_cached = it.cls;
+                }
+                T = OpTable{trow, tent, tval};
+            }
             switch (C.k * 2 + C.kind) {
-                case 2: pass_tile<1, 4, false>(it, C, in_sel, smem, ctr, err); break;
-                case 3: pass_tile<1, 4, true>(it, C, in_sel, smem, ctr, err); break;
-                case 4: pass_tile<2, 4, false>(it, C, in_sel, smem, ctr, err); break;
-                case 5: pass_tile<2, 4, true>(it, C, in_sel, smem, ctr, err); break;
-                case 6: pass_tile<3, 4, false>(it, C, in_sel, smem, ctr, err); break;
-                case 7: pass_tile<3, 4, true>(it, C, in_sel, smem, ctr, err); break;
-                case 8: pass_tile<4, 2, false>(it, C, in_sel, smem, ctr, err); break;
-                case 9: pass_tile<4, 2, true>(it, C, in_sel, smem, ctr, err); break;
-                case 10: pass_tile<5, 2, false>(it, C, in_sel, smem, ctr, err); break;
-                case 11: pass_tile<5, 2, true>(it, C, in_sel, smem, ctr, err); break;
+                case 2: pass_tile<1, 4, false>(it, C, T, in_sel, tile, ctr, err); break;
+                case 3: pass_tile<1, 4, true>(it, C, T, in_sel, tile, ctr, err); break;
+                case 4: pass_tile<2, 4, false>(it, C, T, in_sel, tile, ctr, err); break;
+                case 5: pass_tile<2, 4, true>(it, C, T, in_sel, tile, ctr, err); break;
+                case 6: pass_tile<3, 4, false>(it, C, T, in_sel, tile, ctr, err); break;
+                case 7: pass_tile<3, 4, true>(it, C, T, in_sel, tile, ctr, err); break;
+                case 8: pass_tile<4, 2, false>(it, C, T, in_sel, tile, ctr, err); break;
+                case 9: pass_tile<4, 2, true>(it, C, T, in_sel, tile, ctr, err); break;
+                case 10: pass_tile<5, 2, false>(it, C, T, in_sel, tile, ctr, err); break;
+                case 11: pass_tile<5, 2, true>(it, C, T, in_sel, tile, ctr, err); break;
                 default: break;
             }
         }
@@ -350,11 +377,11 @@ __global__ void __launch_bounds__(kMFThreads, 6)
 int mf_columns_per_thread(int k) { return k <= 3 ? 4 : 2; }
 
 cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,
-                            int in_sel, int* err, size_t smem, int grid, cudaStream_t st) {
+                            int in_sel, int* err, size_t smem, int table_bytes, int grid, cudaStream_t st) {
     if (nitems <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(int) * (size_t)nctr, st);
     if (e != cudaSuccess) return e;
-    k_mf_stage<<<grid, kMFThreads, smem, st>>>(items, nitems, classes, ctr, stage, in_sel, err);
+    k_mf_stage<<<grid, kMFThreads, smem, st>>>(items, nitems, classes, ctr, stage, in_sel, err, table_bytes);
     return cudaGetLastError();
 }
 

@@ -15,7 +15,7 @@
 namespace sgdg {
 
 cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,
-                            int in_sel, int* err, size_t smem, int grid, cudaStream_t st);
+                            int in_sel, int* err, size_t smem, int table_bytes, int grid, cudaStream_t st);
 cudaError_t mf_configure(size_t smem, int* blocks_per_sm);
 int mf_columns_per_thread(int k);
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
@@ -118,8 +118,11 @@ const MFEngine::STable& MFEngine::stab(int k, int n) {
     const MFOperator M = mf_operator(k, n);
     STable S;
     S.rowptr = upload(M.rowptr, stream_);
-    S.colblk = upload(M.colblk, stream_);
+    S.ent = upload(M.ent, stream_);
     S.val = upload(M.val, stream_);
+    S.nrow = (int)M.rowptr.size();
+    S.nent = (int)M.ent.size();
+    S.nval = (int)M.val.size();
     CK(cudaStreamSynchronize(stream_));
     return stabs_.emplace(key, std::move(S)).first->second;
 }
@@ -237,8 +240,12 @@ void MFEngine::plan() {
         const STable& S = stab(s0.spec.k, s0.spec.n);
         MFClass m{};
         m.s_rowptr = S.rowptr.as<int32_t>();
-        m.s_colblk = S.colblk.as<int32_t>();
+        m.s_ent = S.ent.as<int32_t>();
         m.s_val = S.val.as<float>();
+        m.s_nrow = S.nrow;
+        m.s_nent = S.nent;
+        m.s_nval = S.nval;
+        m.s_shared = mf_table_bytes(S.nrow, S.nent, S.nval) <= kMFTableSmemMax;
         m.blockoff = c.blockoff.as<int64_t>();
         m.y = c.y.as<double>();
         m.acc = c.acc.as<double>();
@@ -379,7 +386,16 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
                 items.push_back(it);
             }
         }
-    if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "pencil tile exceeds shared memory");
+    int tb = 0;
+    for (auto& cp : classes_) {
+        const SolveSpec& sp = solves_[cp->slots[0]].spec;
+        const STable& S = stab(sp.k, sp.n);
+        const int b = mf_table_bytes(S.nrow, S.nent, S.nval);
+        if (b <= kMFTableSmemMax) tb = std::max(tb, b);
+    }
+    table_bytes_ = tb;
+    smem += (size_t)tb;
+    if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "operator table and pencil tile exceed shared memory");
     smem_ = smem;
 }
 
@@ -395,7 +411,7 @@ void MFEngine::capture() {
     cudaError_t err = cudaSuccess;
     for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
         err = launch_mf_stage(items_d_.as<MFItem>(), nitems_, classes_d_.as<MFClass>(), ctr_d_.as<int>(), nctr_, stage,
-                              (stage - 1) % 2, err_d_.as<int>(), smem_, grid_, cs);
+                              (stage - 1) % 2, err_d_.as<int>(), smem_, table_bytes_, grid_, cs);
     cudaError_t e2 = cudaStreamEndCapture(cs, &g);
     if (own) cudaStreamDestroy(own);
     if (err != cudaSuccess || e2 != cudaSuccess) {
@@ -499,7 +515,7 @@ void MFEngine::apply(const double* x_dev, double* y_dev) {
     const ClassArena& c = *classes_[0];
     CK(launch_f64_to_f32(x_dev, c.u0.as<float>(), c.N, stream_));
     CK(launch_mf_stage(items_d_.as<MFItem>(), nitems_, classes_d_.as<MFClass>(), ctr_d_.as<int>(), nctr_, 1, 0,
-                       err_d_.as<int>(), smem_, grid_, stream_));
+                       err_d_.as<int>(), smem_, table_bytes_, grid_, stream_));
     CK(launch_f32_to_f64(c.rhs.as<float>(), y_dev, c.N, stream_));
 }
 

@@ -63,7 +63,8 @@ class MFEngine {
         std::vector<double> pending;  // host state not yet on the device
     };
     struct STable {
-        DevBuf rowptr, colblk, val;
+        DevBuf rowptr, ent, val;
+        int nrow = 0, nent = 0, nval = 0;
     };
     struct ClassArena {
         std::tuple<int, int, int, int, int, bool, int> key;
@@ -91,6 +92,7 @@ class MFEngine {
     int nitems_ = 0, nctr_ = 0, grid_ = 0;
     int64_t pending_bytes_ = 0;  // admitted but not yet allocated
     size_t smem_ = 0;
+    int table_bytes_ = 0;  // shared-memory operator table reserved ahead of the tile
     bool dirty_ = true;
     cudaGraphExec_t graph_ = nullptr;
 };

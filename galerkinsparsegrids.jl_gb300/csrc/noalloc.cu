@@ -37,7 +37,7 @@
 
 namespace sgdg {
 cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,
-                            int in_sel, int* err, size_t smem, int grid, cudaStream_t st);
+                            int in_sel, int* err, size_t smem, int table_bytes, int grid, cudaStream_t st);
 cudaError_t mf_configure(size_t smem, int* blocks_per_sm);
 int mf_columns_per_thread(int k);
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
@@ -169,7 +169,11 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
             for (auto& it : items) it.wait_need = it.wait_ctr >= 0 ? count[it.wait_ctr] : 0;
         }
         const int nctr = 1 + (int)dims.size();
-        if (smem > 227 * 1024) return noalloc_fail(SGDG_EUNSUPPORTED, "pencil tile exceeds shared memory");
+        const int tb = mf_table_bytes((int)M.rowptr.size(), (int)M.ent.size(), (int)M.val.size());
+        const int table_bytes = tb <= kMFTableSmemMax ? tb : 0;
+        smem += (size_t)table_bytes;
+        if (smem > 227 * 1024)
+            return noalloc_fail(SGDG_EUNSUPPORTED, "operator table and pencil tile exceed shared memory");
 
         // scratch layout
         Layout L;
@@ -178,7 +182,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         const Region r_ctr = L.add(sizeof(int) * nctr);
         const Region r_err = L.add(sizeof(int));
         const Region r_rowptr = L.add(sizeof(int32_t) * op->rowptr.size());
-        const Region r_colblk = L.add(sizeof(int32_t) * op->colblk.size());
+        const Region r_ent = L.add(sizeof(int32_t) * op->ent.size());
         const Region r_sval = L.add(sizeof(float) * sval.size());
         const Region r_boff = L.add(sizeof(int64_t) * boff.size());
         const Region r_coef = L.add(sizeof(float) * 8);
@@ -198,8 +202,12 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
 
         MFClass c{};
         c.s_rowptr = reinterpret_cast<const int32_t*>(base + r_rowptr.off);
-        c.s_colblk = reinterpret_cast<const int32_t*>(base + r_colblk.off);
+        c.s_ent = reinterpret_cast<const int32_t*>(base + r_ent.off);
         c.s_val = reinterpret_cast<const float*>(base + r_sval.off);
+        c.s_nrow = (int)M.rowptr.size();
+        c.s_nent = (int)M.ent.size();
+        c.s_nval = (int)M.val.size();
+        c.s_shared = table_bytes > 0;
         c.blockoff = reinterpret_cast<const int64_t*>(base + r_boff.off);
         c.y = nullptr;
         c.acc = nullptr;
@@ -229,7 +237,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         const Copy copies[] = {{r_cls, &c},
                                {r_items, items.data()},
                                {r_rowptr, op->rowptr.data()},
-                               {r_colblk, op->colblk.data()},
+                               {r_ent, op->ent.data()},
                                {r_sval, sval.data()},
                                {r_boff, boff.data()},
                                {r_coef, coef},
@@ -250,7 +258,8 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
             e = launch_mf_stage(reinterpret_cast<const MFItem*>(base + r_items.off), (int)items.size(),
                                 reinterpret_cast<const MFClass*>(base + r_cls.off),
                                 reinterpret_cast<int*>(base + r_ctr.off), nctr, 1, 0,
-                                reinterpret_cast<int*>(base + r_err.off), smem, std::max(1, bps) * sms, st);
+                                reinterpret_cast<int*>(base + r_err.off), smem, table_bytes, std::max(1, bps) * sms,
+                                st);
         if (e == cudaSuccess) e = launch_f32_to_f64(c.rhs, y_dev, N, st);
         int err = 0;
         if (e == cudaSuccess) e = cudaMemcpyAsync(&err, base + r_err.off, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -72,11 +72,16 @@ std::shared_ptr<const DLF1D> dlf1d(int k, int n);
 // the coarse function; the reference's structural pattern keeps such blocks
 // as numerical zeros (the plain CSR form keeps them too).  Blocks are dropped
 // when their largest entry is below 1e-10 of the operator's largest entry;
-// zero blocks sit below 1e-13 and kept ones above 1e-3 of it.
+// zero blocks sit below 1e-13 and kept ones above 1e-3 of it.  The kept
+// blocks repeat (the periodic operator is translation invariant and the
+// surviving fine/coarse pairs sit at a few positions relative to a break):
+// k=3, n=7 keeps 1568 blocks but only 163 distinct ones, so the table stores
+// distinct blocks once and each row lists (column block << 12 | block id).
 struct MFOperator {
-    int k = 0, n = 0, rs = 0;
-    std::vector<int32_t> rowptr, colblk;
-    std::vector<float> val;
+    int k = 0, n = 0, rs = 0, ndist = 0;
+    std::vector<int32_t> rowptr;  // 2^n + 1
+    std::vector<int32_t> ent;     // per row, sorted by column block
+    std::vector<float> val;       // ndist blocks of k rows x rs floats
 };
 MFOperator mf_operator(int k, int n);
 
