@@ -42,7 +42,7 @@ def _method(method):
 
 # ---------------------------------------------------------------- layout ----
 def get_size(D, k, n, scheme="sparse"):
-    """Number of coefficients (src/dg_vmethods.jl:179-189)."""
+    """Number of coefficients (src/dg_vmethods.jl:35-45)."""
     N = ctypes.c_int64()
     check(lib().sgdg_get_size(D, k, n, _scheme(scheme), ctypes.byref(N)))
     return N.value
@@ -59,18 +59,18 @@ def index_map(D, k, n, scheme="sparse"):
 
 
 def V2Dref(D, k, n, scheme="sparse"):
-    """Vector of (level, cell, mode) tuples (src/dg_vmethods.jl:267-286)."""
+    """Vector of (level, cell, mode) tuples (src/dg_vmethods.jl:123-142)."""
     L, C, M = index_map(D, k, n, scheme)
     return [(tuple(L[i]), tuple(C[i]), tuple(M[i])) for i in range(L.shape[0])]
 
 
 def D2Vref(D, k, n, scheme="sparse"):
-    """Dict (level, cell, mode) -> 1-based vector index (src/dg_vmethods.jl:246-265)."""
+    """Dict (level, cell, mode) -> 1-based vector index (src/dg_vmethods.jl:102-121)."""
     return {t: i + 1 for i, t in enumerate(V2Dref(D, k, n, scheme))}
 
 
 def V2D(D, k, n, vect, scheme="sparse"):
-    """Vector -> {level: {cell: {mode: value}}} (src/dg_vmethods.jl:220-244)."""
+    """Vector -> {level: {cell: {mode: value}}} (src/dg_vmethods.jl:76-100)."""
     out = {}
     for (lv, cl, md), val in zip(V2Dref(D, k, n, scheme), vect):
         out.setdefault(lv, {}).setdefault(cl, {})[md] = val
@@ -78,12 +78,12 @@ def V2D(D, k, n, vect, scheme="sparse"):
 
 
 def D2V(D, k, n, coeffs, scheme="sparse"):
-    """Inverse of V2D (src/dg_vmethods.jl:192-217)."""
+    """Inverse of V2D (src/dg_vmethods.jl:48-74)."""
     return np.array([coeffs[lv][cl][md] for (lv, cl, md) in V2Dref(D, k, n, scheme)])
 
 
 def dg_coeffs(k):
-    """dg_coeffs[k] (src/1d_dg_functions.jl:243-253) as a (2k, k) array."""
+    """dg_coeffs[k] (src/1d_dg_functions.jl:52-62) as a (2k, k) array."""
     out = np.zeros(2 * k * k)
     check(lib().sgdg_dg_coeffs(k, out))
     return out.reshape(k, 2 * k).T.copy()
@@ -143,7 +143,7 @@ def vcoeffs_1d(k, n, f, q=None):
 
 
 def vcoeffs_DG(D, k, n, f, scheme="sparse", q=None):
-    """Coefficient vector of f (src/dg_vmethods.jl:293-323).
+    """Coefficient vector of f (src/dg_vmethods.jl:149-179).
 
     ``f`` takes an (npts, D) array of points and returns npts values.  The
     reference integrates each basis function with hcubature; here every level
@@ -193,7 +193,7 @@ def _i1d(k, L, C, M):
 
 def tensor_construct(D, k, n, vcoeff_array, scheme="sparse"):
     """Coefficients of prod_d f_d(x_d) from 1D coefficient vectors
-    (src/tensor_construct.jl:323-329)."""
+    (src/tensor_construct.jl:57-63)."""
     L, C, M = index_map(D, k, n, scheme)
     out = np.ones(L.shape[0])
     for q in range(D):
@@ -296,7 +296,7 @@ class SparseGridOperator:
 
 
 def D_matrix(D, d, k, n, scheme="sparse"):
-    """D-dimensional derivative along dim d, 1-based (src/multidim_derivative.jl:209-213)."""
+    """D-dimensional derivative along dim d, 1-based (src/multidim_derivative.jl:61-65)."""
     return SparseGridOperator(D, k, n, scheme).csr(d)
 
 
@@ -354,7 +354,7 @@ def wave_evolve(D, k, n, f0, v0, time0, time1, order="rk4", scheme="sparse", dt=
 def advect_evolve(D, k, n, a, f0, time0, time1, order="rk4", scheme="sparse", dt=None, nsteps=None, nout=2,
                   method="plain", op=None):
     """f_t = -sum_d a_d D_d f on the periodic unit cube (operator composed
-    from grad_matrix, src/multidim_derivative.jl:215-217).  Returns (times, states)."""
+    from grad_matrix, src/multidim_derivative.jl:67-69).  Returns (times, states)."""
     _order(order)
     if callable(f0):
         f0 = vcoeffs_DG(D, k, n, f0, scheme)

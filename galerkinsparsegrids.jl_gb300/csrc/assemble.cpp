@@ -1,6 +1,6 @@
 // assemble.cpp -- assembled (plain-form) operators in CSR.
 //
-// D_d follows src/multidim_derivative.jl:167-206: the entry (i, j) exists when
+// D_d follows src/multidim_derivative.jl:19-58: the entry (i, j) exists when
 // i and j agree in every dimension but d and their dim-d triples are a stored
 // pair of the 1D operator, and row i's level tuple is not cut; its value is
 // the 1D entry.  Rows are produced directly (CSR) with columns sorted, which is
@@ -8,7 +8,7 @@
 // stored entries (numerical zeros included).
 //
 // Sums and products keep the structural pattern.  The reference's
-// laplacian_matrix (src/multidim_derivative.jl:219-227) adds with
+// laplacian_matrix (src/multidim_derivative.jl:71-79) adds with
 // SparseArrays' map(+), which also drops entries whose floating-point sum is
 // exactly 0.0; which entries cancel exactly depends on the roundoff of its
 // quadrature, so that subset cannot be reproduced by any other

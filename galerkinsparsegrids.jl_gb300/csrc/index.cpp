@@ -4,7 +4,7 @@
 // boundary without permutation): level tuples in Julia CartesianIndices order
 // with dimension 1 fastest, skipping tuples with sum(L) > n + D for the
 // sparse scheme (src/schemes.jl:21-27); inside a level block, cells then
-// modes, each column-major (src/dg_vmethods.jl:246-286).
+// modes, each column-major (src/dg_vmethods.jl:102-142).
 #include "sgdg_core.h"
 
 namespace sgdg {

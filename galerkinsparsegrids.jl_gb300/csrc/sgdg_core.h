@@ -12,7 +12,7 @@
 
 namespace sgdg {
 
-constexpr int kKMax = 10;  // K_max, src/1d_dg_functions.jl:198
+constexpr int kKMax = 10;  // K_max, src/1d_dg_functions.jl:7
 constexpr int kDMax = 8;   // largest dimension the library indexes
 
 struct Error : std::runtime_error {
@@ -86,7 +86,7 @@ struct MFOperator {
 MFOperator mf_operator(int k, int n);
 
 // ------------------------------------------------------------ index map ----
-// Sparse-grid coefficient layout of src/dg_vmethods.jl:246-286: level tuples
+// Sparse-grid coefficient layout of src/dg_vmethods.jl:102-142: level tuples
 // in Julia CartesianIndices order (dimension 1 fastest), then cells, then modes.
 struct SparseIndex {
     int D = 0, k = 0, n = 0, scheme = 0;

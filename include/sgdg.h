@@ -9,7 +9,7 @@
  *    Nothing throws or aborts across this boundary.
  *  - Coefficient vectors use the reference's layout exactly (levels in
  *    column-major CartesianIndices order, then cells, then modes;
- *    src/dg_vmethods.jl:246-286), so a Julia Vector{Float64} from vcoeffs_DG
+ *    src/dg_vmethods.jl:102-142), so a Julia Vector{Float64} from vcoeffs_DG
  *    passes through unchanged.  Arrays are caller-owned; pointers named *_dev
  *    are device pointers, all others are host memory.
  *  - Indices in exported CSR arrays are 0-based; level/cell/mode in
@@ -59,12 +59,12 @@ int sgdg_version(char *buf, size_t len);
 int sgdg_last_error(char *buf, size_t len);
 
 /* ---- index map ---------------------------------------------------------- */
-/* get_size (src/dg_vmethods.jl:179-189). */
+/* get_size (src/dg_vmethods.jl:35-45). */
 int sgdg_get_size(int D, int k, int n, int scheme, int64_t *N);
-/* V2Dref (src/dg_vmethods.jl:267-286): N x D arrays (row-major, entry [i*D+q])
+/* V2Dref (src/dg_vmethods.jl:123-142): N x D arrays (row-major, entry [i*D+q])
  * of 1-based level, cell and mode of every coefficient. */
 int sgdg_index_map(int D, int k, int n, int scheme, int32_t *level, int32_t *cell, int32_t *mode);
-/* dg_coeffs[k] (src/1d_dg_functions.jl:243-253): 2k x k, column-major
+/* dg_coeffs[k] (src/1d_dg_functions.jl:52-62): 2k x k, column-major
  * (out[mode*2k + i]; i < k: x^i, i >= k: sgn(x) x^(i-k)). */
 int sgdg_dg_coeffs(int k, double *out);
 
@@ -75,7 +75,7 @@ int sgdg_dlf_1d_export(int k, int n, int64_t *rowptr, int32_t *col, double *val)
 
 /* ---- operators ---------------------------------------------------------- */
 /* Operator handle for (D, k, n, scheme); replaces the setup of
- * D_matrix / grad_matrix / laplacian_matrix (src/multidim_derivative.jl:209-227).
+ * D_matrix / grad_matrix / laplacian_matrix (src/multidim_derivative.jl:61-79).
  * Requires n >= 2 and 1 <= k <= 10. */
 int sgdg_op_create(int D, int k, int n, int scheme, sgdg_op **out);
 int sgdg_op_destroy(sgdg_op *op);

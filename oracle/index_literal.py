@@ -1,7 +1,7 @@
 """Pure-Python, loop-for-loop restatement of the reference's dictionary <-> vector
 coefficient layout, for small cases only.
 
-TEST INFRASTRUCTURE ONLY.  Follows src/dg_vmethods.jl:179-286 (get_size, D2V,
+TEST INFRASTRUCTURE ONLY.  Follows src/dg_vmethods.jl:35-142 (get_size, D2V,
 V2D, D2Vref, V2Dref) and src/schemes.jl:21-27 (cutoff), including Julia's
 column-major CartesianIndices order (dimension 1 fastest) and 1-based levels.
 Dictionaries are keyed by 1-based level tuples; each value is a dict keyed by
@@ -81,7 +81,7 @@ def D2V(D, k, n, coeffs, scheme="sparse"):
 
 
 def get_index_1D(k, l, c, m):
-    """src/additional_tools.jl:119-121; for l = 1 the Julia shift by
+    """src/additional_tools.jl:18-20; for l = 1 the Julia shift by
     (l-2)%UInt wraps past the word size and yields 0."""
     shift = (1 << (l - 2)) if l >= 2 else 0
     return k * (shift + (c - 1)) + m

@@ -126,7 +126,7 @@ def _scheme(scheme):
 
 # --- basis (src/dg_basis.jl, src/1d_dg_functions.jl) -------------------------
 def dg_coeffs(k):
-    """dg_coeffs[k] as a (2k, k) array: column = mode (src/1d_dg_functions.jl:243-253)."""
+    """dg_coeffs[k] as a (2k, k) array: column = mode (src/1d_dg_functions.jl:52-62)."""
     out = np.zeros(2 * k * k)
     lib().or_dg_coeffs(k, out)
     return out.reshape(k, 2 * k).T.copy()
@@ -176,7 +176,7 @@ def periodic_DLF_matrix(k, n):
 
 
 def D_matrix(D, d, k, n, scheme="sparse"):
-    """D-dim derivative along dim d, 1-based (src/multidim_derivative.jl:209-213)."""
+    """D-dim derivative along dim d, 1-based (src/multidim_derivative.jl:61-65)."""
     return _Mat(lib().or_dmatrix(D, d, k, n, _scheme(scheme))).csc()
 
 
@@ -293,7 +293,7 @@ def reconstruct(D, k, n, coeffs, pts, scheme="sparse"):
 
 def vcoeffs_1d(k, n, f, q=24):
     """1D hierarchical coefficients of a vectorised f by Gauss-Legendre per
-    polynomial piece (the oracle's stand-in for hquadrature, dg_vmethods.jl:299-323)."""
+    polynomial piece (the oracle's stand-in for hquadrature, dg_vmethods.jl:149-179)."""
     gx, gw = np.polynomial.legendre.leggauss(q)
     out = []
     for L in range(1, n + 2):

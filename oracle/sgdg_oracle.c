@@ -9,16 +9,16 @@
  * where the reference fixes one (compiled with -ffp-contract=off, no FMA):
  *   - src/dg_basis.jl:21-190          product_matrix, inner_product, Gram-Schmidt,
  *                                      legendre, orthogonalize_1/2, dg_basis
- *   - src/1d_dg_functions.jl:206-260  array2poly, LegendreP, dg_coeffs, h
- *   - src/1d_dg_functions.jl:274-308  leg, basis, pos_vcoeffs_DG
- *   - src/1d_dg_functions.jl:433-454  hier2pos (matrix form)
+ *   - src/1d_dg_functions.jl:15-74  array2poly, LegendreP, dg_coeffs, h
+ *   - src/1d_dg_functions.jl:83-117  leg, basis, pos_vcoeffs_DG
+ *   - src/1d_dg_functions.jl:242-263  hier2pos (matrix form)
  *   - src/dg_methods.jl:27-36         v (hierarchical basis)
- *   - src/derivative_matrix_elements.jl:245-277  symbolic_diff, legendreDlegendre, legvDv
+ *   - src/derivative_matrix_elements.jl:80-112  symbolic_diff, legendreDlegendre, legvDv
  *   - src/1d_derivative.jl:21-117     D_matrix(k,level), periodic_legvLFv, periodic_LF_matrix,
  *                                      periodic_pos_DLF_matrix, periodic_hier_DLF_matrix
- *   - src/schemes.jl:21-27, src/dg_vmethods.jl:179-286, src/additional_tools.jl:109-121
+ *   - src/schemes.jl:21-27, src/dg_vmethods.jl:35-142, src/additional_tools.jl:8-20
  *                                      cutoff, get_size, D2Vref/V2Dref ordering, get_index_1D
- *   - src/multidim_derivative.jl:167-227  D_matrix(Val(d),...), grad_matrix, laplacian_matrix
+ *   - src/multidim_derivative.jl:19-79  D_matrix(Val(d),...), grad_matrix, laplacian_matrix
  *   - src/pdes.jl:22-49               wave_data
  * and the Julia SparseArrays semantics those files rely on:
  *   sparse(I,J,V,m,n,+) keeps numerical zeros; SpGEMM (Gustavson) keeps
@@ -41,7 +41,7 @@
 
 #include "sgdg_oracle.h"
 
-#define KMAX 10          /* K_max, src/1d_dg_functions.jl:198 */
+#define KMAX 10          /* K_max, src/1d_dg_functions.jl:7 */
 #define LEGN (2 * (KMAX + 1))
 
 static double g_leg[KMAX + 1][LEGN];         /* leg_coeffs = legendre(K_max)      */
@@ -188,7 +188,7 @@ void or_leg_coeffs(double *out) { /* out[m*22 + coef], m = 0..10 */
 }
 
 /* ------------------------------------------------------------------------- */
-/* Basis evaluation: src/1d_dg_functions.jl:206-219,229-231,257-260,274-284   */
+/* Basis evaluation: src/1d_dg_functions.jl:15-32,38-46,66-74,83-97   */
 /* ------------------------------------------------------------------------- */
 static double array2poly(const double *v, int n, double x) {
     if (fabs(x) > 1) return 0.0;
@@ -210,7 +210,7 @@ double or_v(int k, int level, int cell, int mode, double x) {
     return h_fn(k, mode, (double)(1LL << level) * x - (double)(2 * cell - 1)) * sqrt(1.0 * (double)(1LL << level));
 }
 
-/* src/1d_dg_functions.jl:274-284 */
+/* src/1d_dg_functions.jl:83-97 */
 static double leg(int mode, double x) { return sqrt(2.0) * LegendreP(mode - 1, 2 * x - 1); }
 double or_basis(int level, int cell, int mode, double x) {
     return leg(mode, (double)(1LL << level) * x - (double)(cell - 1)) * pow(2.0, (double)level / 2.0);
@@ -476,7 +476,7 @@ static or_mat *map_add(const or_mat *A, const or_mat *B, double sa, double sb) {
 /* 1D operators                                                               */
 /* ------------------------------------------------------------------------- */
 
-/* src/1d_dg_functions.jl:433-454: Q[pos(cell,p), hier(level,cell,mode)] by
+/* src/1d_dg_functions.jl:242-263: Q[pos(cell,p), hier(level,cell,mode)] by
  * quadrature over each finest cell; entries with |val| > atol=1e-12 kept. */
 or_mat *or_hier2pos(int k, int n) {
     or_init();
@@ -511,7 +511,7 @@ or_mat *or_hier2pos(int k, int n) {
     return Q;
 }
 
-/* src/derivative_matrix_elements.jl:245-259 */
+/* src/derivative_matrix_elements.jl:80-94 */
 static void symbolic_diff(const double *v, int n, double *ans) {
     int k = n / 2;
     for (int i = 1; i <= n; i++) {
@@ -524,14 +524,14 @@ static void symbolic_diff(const double *v, int n, double *ans) {
     }
 }
 
-/* src/derivative_matrix_elements.jl:266-268 */
+/* src/derivative_matrix_elements.jl:101-103 */
 static double legendreDlegendre(int m1, int m2) {
     double d[LEGN];
     symbolic_diff(g_leg[m2 - 1], LEGN, d);
     return inner_vv(g_leg[m1 - 1], d, LEGN);
 }
 
-/* src/1d_derivative.jl:21-44 with legvDv (derivative_matrix_elements.jl:271-277) */
+/* src/1d_derivative.jl:21-44 with legvDv (derivative_matrix_elements.jl:106-112) */
 static or_mat *pos_D_matrix(int k, int level) {
     coo_t c = {0};
     int ncell = 1 << level;
@@ -624,7 +624,7 @@ or_mat *or_dmat1d(int k, int n) {
 }
 
 /* ------------------------------------------------------------------------- */
-/* Sparse-grid index map: src/schemes.jl:21-27, src/dg_vmethods.jl:179-286    */
+/* Sparse-grid index map: src/schemes.jl:21-27, src/dg_vmethods.jl:35-142    */
 /* ------------------------------------------------------------------------- */
 typedef struct {
     int D, k, n, scheme;
@@ -754,7 +754,7 @@ void or_index_map(int D, int k, int n, int scheme, int32_t *Lout, int32_t *Cout,
 }
 
 /* ------------------------------------------------------------------------- */
-/* D-dimensional derivative: src/multidim_derivative.jl:167-206               */
+/* D-dimensional derivative: src/multidim_derivative.jl:19-58               */
 /* ------------------------------------------------------------------------- */
 static or_mat *dmatrix_from_1d(const or_mat *Dm1, int D, int d, int k, int n, int scheme) {
     idx_t ix;
@@ -782,7 +782,7 @@ static or_mat *dmatrix_from_1d(const or_mat *Dm1, int D, int d, int k, int n, in
     for (int64_t j = 0; j < ix.N; j++) {
         const int32_t *L = Lv + j * D, *C = Cv + j * D, *M = Mv + j * D;
         int l = L[d - 1], c = C[d - 1], m = M[d - 1];
-        /* get_index_1D (additional_tools.jl:119-121), 0-based */
+        /* get_index_1D (additional_tools.jl:18-20), 0-based */
         int64_t j1 = (int64_t)k * ((l >= 2 ? (1LL << (l - 2)) : 0) + (c - 1)) + (m - 1);
         for (int q = 0; q < D; q++) {
             L2[q] = L[q];
@@ -819,7 +819,7 @@ or_mat *or_dmatrix(int D, int d, int k, int n, int scheme) {
     return R;
 }
 
-/* src/multidim_derivative.jl:219-227: lap = spzeros; lap += D_d * D_d */
+/* src/multidim_derivative.jl:71-79: lap = spzeros; lap += D_d * D_d */
 or_mat *or_laplacian(int D, int k, int n, int scheme) {
     or_init();
     or_mat *Dm1 = or_dmat1d(k, n);
@@ -852,7 +852,7 @@ or_mat *or_wave_rhs(const or_mat *lap) {
 }
 
 /* Advection operator -sum_d a_d D_d (composition of grad_matrix,
- * multidim_derivative.jl:215-217, assembled like laplacian_matrix's sum). */
+ * multidim_derivative.jl:67-69, assembled like laplacian_matrix's sum). */
 or_mat *or_advection(int D, int k, int n, int scheme, const double *a) {
     or_init();
     or_mat *Dm1 = or_dmat1d(k, n);
@@ -987,8 +987,8 @@ int or_max_threads(void) {
 }
 
 /* ------------------------------------------------------------------------- */
-/* Projection and reconstruction helpers (src/dg_vmethods.jl:299-323,        */
-/* src/tensor_construct.jl:289-329, src/dg_methods.jl:150-165)               */
+/* Projection and reconstruction helpers (src/dg_vmethods.jl:149-179,        */
+/* src/tensor_construct.jl:19-63, src/dg_methods.jl:150-165)               */
 /* ------------------------------------------------------------------------- */
 
 /* 1D coefficients of exp(2*pi*i*a*x) on the hierarchical basis, in 1D vector
@@ -1063,7 +1063,7 @@ void or_fourier_coeffs(int D, int k, int n, int scheme, int nmodes, const int32_
     idx_free(&ix);
 }
 
-/* tensor_construct (src/tensor_construct.jl:289-329): coefficient of
+/* tensor_construct (src/tensor_construct.jl:19-63): coefficient of
  * prod_d f_d(x_d) from the 1D coefficient vectors coeffs1d[d*len1 + j1]. */
 void or_tensor_construct(int D, int k, int n, int scheme, const double *coeffs1d, double *out) {
     idx_t ix;

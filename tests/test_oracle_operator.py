@@ -35,7 +35,7 @@ def test_1d_operator_is_skew(O, k, n):
 
 @pytest.mark.parametrize("D,d,k,n", [(2, 1, 3, 5), (2, 2, 3, 5), (3, 2, 2, 4), (3, 3, 3, 3)])
 def test_dd_pattern_is_lines_of_1d_pattern(O, D, d, k, n):
-    # src/multidim_derivative.jl:180-205: column j copies the 1D column of its
+    # src/multidim_derivative.jl:32-55: column j copies the 1D column of its
     # dim-d triple into dim d, skipping cut rows.
     Dd = O.D_matrix(D, d, k, n).tocoo()
     L, C, M = O.index_map(D, k, n)
