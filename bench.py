@@ -137,7 +137,7 @@ def measured_peak_hbm():
 
 def profiled_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_mf_pass_wave3d.json")
+    path = os.path.join(ROOT, "profiles", "k_mf_stage_wave3d.json")
     try:
         with open(path) as f:
             return json.load(f)

@@ -121,8 +121,9 @@ int sgdg_advect_evolve(sgdg_op *op, const double *a, const double *f0, double t0
 
 /* ---- batches of independent solves (matrix-free form) ------------------- */
 /* Many solves of uneven D, k, n advance together: each RK stage is one
- * launch per dimension over the tiles of every solve, replayed from a CUDA
- * graph.  State stays on the device between calls. */
+ * persistent launch over the pencil tiles and RK chunks of every solve, and
+ * one RK4 step is replayed from a CUDA graph.  State stays on the device
+ * between calls. */
 int sgdg_batch_create(sgdg_batch **out);
 int sgdg_batch_destroy(sgdg_batch *b);
 /* Adds a solve; y0 has N (advection) or 2N (wave: [f; v]) coefficients;
