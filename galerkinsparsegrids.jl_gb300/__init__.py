@@ -389,8 +389,8 @@ def energy_func(D, k, n, soln, scheme="sparse", op=None):
 # --------------------------------------------------------------- batches ----
 class Batch:
     """Independent solves of uneven (D, k, n) advanced together by the
-    matrix-free FP32/FP64 engine (one launch per dimension per RK stage,
-    replayed from a CUDA graph)."""
+    matrix-free FP32/FP64 engine (one persistent launch per RK stage, one RK4
+    step replayed from a CUDA graph)."""
 
     def __init__(self):
         h = ctypes.c_void_p()
@@ -459,6 +459,83 @@ class Batch:
         dofs = ctypes.c_double()
         check(lib().sgdg_batch_step_info(self._h, ctypes.byref(launches), ctypes.byref(dofs)))
         return launches.value, dofs.value
+
+
+# -------------------------------------------------------------- serving ----
+class Server:
+    """Request loop over the matrix-free engine (continuous batching): queued
+    solves are admitted in arrival order while the HBM budget has room, run
+    together in shared launches, and leave when their steps are done.  Times
+    are seconds on the server's steady clock (``clock()``)."""
+
+    QUEUED, RUNNING, DONE, FAILED, CANCELLED = range(5)
+
+    def __init__(self, max_chunk_steps=25):
+        h = ctypes.c_void_p()
+        check(lib().sgdg_server_create(int(max_chunk_steps), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sgdg_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        check(lib().sgdg_server_set_stream(self._h, ctypes.c_void_p(stream)))
+
+    def clock(self):
+        t = ctypes.c_double()
+        check(lib().sgdg_server_clock(self._h, ctypes.byref(t)))
+        return t.value
+
+    def submit(self, kind, D, k, n, y0, dt, nsteps, a=None, scheme="sparse", t_arrival=-1.0):
+        kinds = {"advect": _lib.KIND_ADVECT, "wave": _lib.KIND_WAVE}
+        if kind not in kinds:
+            raise ValueError("kind must be \"advect\" or \"wave\"")
+        y0 = np.ascontiguousarray(y0, np.float64)
+        ap = None
+        if a is not None:
+            a_arr = np.ascontiguousarray(a, np.float64)
+            ap = a_arr.ctypes.data_as(ctypes.c_void_p)
+        rid = ctypes.c_int64()
+        check(lib().sgdg_server_submit(self._h, kinds[kind], D, k, n, _scheme(scheme), ap, float(dt), y0,
+                                       int(nsteps), float(t_arrival), ctypes.byref(rid)))
+        return rid.value
+
+    def tick(self):
+        """One admit / advance / retire round; returns the number finished."""
+        c = ctypes.c_int()
+        check(lib().sgdg_server_tick(self._h, ctypes.byref(c)))
+        return c.value
+
+    def status(self, rid):
+        """(state, steps_done, t_arrival, t_admit, t_done)."""
+        st, sd = ctypes.c_int(), ctypes.c_int64()
+        ta, tb, tc = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().sgdg_server_status(self._h, int(rid), ctypes.byref(st), ctypes.byref(sd), ctypes.byref(ta),
+                                       ctypes.byref(tb), ctypes.byref(tc)))
+        return st.value, sd.value, ta.value, tb.value, tc.value
+
+    def result(self, rid, size):
+        y = np.empty(int(size))
+        check(lib().sgdg_server_result(self._h, int(rid), y))
+        return y
+
+    def cancel(self, rid):
+        check(lib().sgdg_server_cancel(self._h, int(rid)))
+
+    def counts(self):
+        """(queued, running, finished not yet collected, DOF-updates so far)."""
+        q, r, f = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        d = ctypes.c_double()
+        check(lib().sgdg_server_counts(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(f), ctypes.byref(d)))
+        return q.value, r.value, f.value, d.value
 
 
 def set_hbm_budget(nbytes):

@@ -23,8 +23,12 @@ EXPORTS = [
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
     "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info",
+    "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
+    "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
+    "sgdg_server_counts",
     "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
 ]
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
 
 
 class SGDGError(RuntimeError):
@@ -76,6 +80,18 @@ def lib(build=True):
     _sig(L, "sgdg_apply_noalloc", [_ci, _ci, _ci, _ci, _ci, _vp, _vp, _vp])
     _sig(L, "sgdg_wave_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
     _sig(L, "sgdg_advect_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
+    _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
+    _sig(L, "sgdg_server_destroy", [_vp])
+    _sig(L, "sgdg_server_set_stream", [_vp, _vp])
+    _sig(L, "sgdg_server_clock", [_vp, ctypes.POINTER(_cd)])
+    _sig(L, "sgdg_server_submit", [_vp, _ci, _ci, _ci, _ci, _ci, _vp, _cd, _f64p, _c64, _cd, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_server_tick", [_vp, ctypes.POINTER(_ci)])
+    _sig(L, "sgdg_server_status", [_vp, _c64, ctypes.POINTER(_ci), ctypes.POINTER(_c64), ctypes.POINTER(_cd),
+                                   ctypes.POINTER(_cd), ctypes.POINTER(_cd)])
+    _sig(L, "sgdg_server_result", [_vp, _c64, _f64p])
+    _sig(L, "sgdg_server_cancel", [_vp, _c64])
+    _sig(L, "sgdg_server_counts", [_vp, ctypes.POINTER(_c64), ctypes.POINTER(_c64), ctypes.POINTER(_c64),
+                                   ctypes.POINTER(_cd)])
     _sig(L, "sgdg_batch_create", [ctypes.POINTER(_vp)])
     _sig(L, "sgdg_batch_destroy", [_vp])
     _sig(L, "sgdg_batch_add", [_vp, _ci, _ci, _ci, _ci, _ci, _vp, _cd, _f64p, ctypes.POINTER(_ci)])

@@ -12,6 +12,7 @@
 #include "../../include/sgdg.h"
 #include "device_util.h"
 #include "engine.h"
+#include "api_util.h"
 #include "mf_engine.h"
 #include "sgdg_core.h"
 
@@ -105,28 +106,6 @@ struct sgdg_batch {
         if (own) cudaStreamDestroy(own);
     }
 };
-
-#define API_BEGIN try {
-#define API_END                                        \
-    return SGDG_OK;                                    \
-    }                                                  \
-    catch (const sgdg::Error& e) {                     \
-        set_error(e.what());                           \
-        return e.code;                                 \
-    }                                                  \
-    catch (const std::bad_alloc&) {                    \
-        set_error("host allocation failed");           \
-        return SGDG_ENOMEM_BUDGET;                     \
-    }                                                  \
-    catch (const std::exception& e) {                  \
-        set_error(e.what());                           \
-        return SGDG_EINVAL;                            \
-    }
-
-#define NEED(p)                                                    \
-    do {                                                           \
-        if (!(p)) throw Error(SGDG_EINVAL, #p " must not be NULL"); \
-    } while (0)
 
 static void copy_str(const std::string& s, char* buf, size_t len) {
     if (!buf || len == 0) return;

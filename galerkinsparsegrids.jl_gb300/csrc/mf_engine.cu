@@ -2,8 +2,9 @@
 //
 // Solves with equal (kind, D, k, n, scheme) share a class: their vectors live
 // in class arenas (slot-major) so pencil tiles can take columns from several
-// solves.  plan() (re)builds classes, arenas and the ordered work list when
-// solves join or leave; states move into the new arenas device-to-device.
+// solves.  plan() rebuilds the arenas of classes whose solves changed (states
+// move into the new arena device-to-device), keeps the others as they are, and
+// rebuilds the ordered work list.
 // One RK4 step is four launches of k_mf_stage (one per stage) captured once in
 // a CUDA graph; a membership change drops the graph and the next step
 // re-captures it.
@@ -62,10 +63,10 @@ int MFEngine::add(const SolveSpec& sp, const double* y0) {
     // admission: the solve's arena share must fit the HBM budget now
     const int64_t need = solve_bytes(s.N, s.Ns);
     const int64_t budget = g_budget.load();
-    if (budget > 0 && g_in_use.load() + pending_bytes_ + need > budget)
+    const int64_t held = g_in_use.load() - dead_bytes() + pending_bytes_;
+    if (budget > 0 && held + need > budget)
         throw Error(SGDG_ENOMEM_BUDGET, "HBM budget: solve needs " + std::to_string(need) + " bytes, " +
-                                            std::to_string(g_in_use.load() + pending_bytes_) + " of " +
-                                            std::to_string(budget) + " committed");
+                                            std::to_string(held) + " of " + std::to_string(budget) + " committed");
     if (y0) s.pending.assign(y0, y0 + s.Ns);
     else s.pending.assign(s.Ns, 0.0);
     solves_.push_back(std::move(s));
@@ -77,6 +78,20 @@ int MFEngine::add(const SolveSpec& sp, const double* y0) {
 int64_t MFEngine::solve_bytes(int64_t N, int64_t Ns) {
     // y, acc (FP64), two stage inputs (FP32), partial sums (FP32)
     return Ns * (8 + 8 + 4 + 4) + N * 4;
+}
+
+int64_t MFEngine::dead_bytes() const {
+    int64_t b = 0;
+    for (auto& s : solves_)
+        if (!s.live && s.cls >= 0) b += solve_bytes(s.N, s.Ns);
+    return b;
+}
+
+int64_t MFEngine::replan_reserve() const {
+    int64_t r = (int64_t)items_d_.bytes + (int64_t)classes_d_.bytes;
+    int64_t ymax = 0;
+    for (auto& c : classes_) ymax = std::max<int64_t>(ymax, (int64_t)c->y.bytes);
+    return r + ymax;
 }
 
 void MFEngine::remove(int id) {
@@ -160,9 +175,19 @@ void MFEngine::plan() {
     std::map<std::tuple<int, int, int, int, int, bool, int>, int> old_of;
     for (size_t oi = 0; oi < classes_.size(); oi++) old_of[classes_[oi]->key] = (int)oi;
     for (size_t ci = 0; ci < next.size(); ci++) {
-        ClassArena& c = *next[ci];
-        auto of = old_of.find(c.key);
+        auto of = old_of.find(next[ci]->key);
         ClassArena* old_c = of == old_of.end() ? nullptr : classes_[of->second].get();
+        if (old_c && old_c->slots == next[ci]->slots) {
+            // same solves in the same slots: keep the arena as it is, unless a
+            // host state is waiting to be uploaded
+            bool pending = false;
+            for (int id : old_c->slots) pending = pending || !solves_[id].pending.empty();
+            if (!pending) {
+                next[ci] = std::move(classes_[of->second]);
+                continue;
+            }
+        }
+        ClassArena& c = *next[ci];
         if (old_c) {  // free what the new arena does not need from the old one first
             old_c->acc.release();
             old_c->u0.release();

@@ -41,6 +41,7 @@ class MFEngine {
     int64_t total_size() const;
 
     void step(int64_t nsteps);                  // RK4 steps of every live solve (async)
+    void flush() { plan(); }                    // applies pending joins and leaves now
     void get_state(int id, double* host);       // synchronises
     void set_state(int id, const double* host); // async (pageable memory is staged)
     void upload_all(const double* host);
@@ -53,6 +54,11 @@ class MFEngine {
     int64_t launches_per_step() const { return 4; }
     int check_error();  // returns SGDG_OK or SGDG_ETIMEOUT after a bounded wait gave up
     static int64_t solve_bytes(int64_t N, int64_t Ns);  // device bytes a solve occupies
+    int64_t pending_bytes() const { return pending_bytes_; }
+    int64_t dead_bytes() const;  // arena shares of removed solves, freed by the next re-plan
+    // device bytes a re-plan holds on top of the steady state: the largest
+    // class's old FP64 state while its new arena is filled, and the old work list
+    int64_t replan_reserve() const;
 
    private:
     struct Solve {

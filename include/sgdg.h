@@ -153,6 +153,46 @@ int sgdg_batch_download(sgdg_batch *b, double *y_all);
  * (32 B per state coefficient per RK stage). */
 int sgdg_batch_step_info(sgdg_batch *b, int64_t *launches_per_step, double *dof_updates_per_step);
 
+/* ---- request loop (continuous batching of matrix-free solves) ------------ */
+/* A server owns one batch engine and a queue.  sgdg_server_tick admits the
+ * queued requests that have arrived, in submission order, while the HBM
+ * budget (sgdg_set_hbm_budget) has room; advances every running request by
+ * the same number of RK4 steps (the fewest any of them has left, at most
+ * max_chunk_steps) in shared persistent launches; and retires the finished
+ * ones, whose states wait on the host for sgdg_server_result.  A request that
+ * cannot fit the budget even alone fails with SGDG_ENOMEM_BUDGET.  Results do
+ * not depend on which other requests ran at the same time.  No counterpart in
+ * the reference (each wave_evolve call there is one blocking solve). */
+typedef struct sgdg_server sgdg_server;
+enum { SGDG_REQ_QUEUED = 0, SGDG_REQ_RUNNING = 1, SGDG_REQ_DONE = 2, SGDG_REQ_FAILED = 3, SGDG_REQ_CANCELLED = 4 };
+int sgdg_server_create(int max_chunk_steps, sgdg_server **out);
+int sgdg_server_destroy(sgdg_server *s);
+/* Use a caller stream (cudaStream_t; NULL = the server's own). */
+int sgdg_server_set_stream(sgdg_server *s, void *stream);
+/* Seconds since the server was created (steady clock); arrival, admission
+ * and completion times are on this clock. */
+int sgdg_server_clock(sgdg_server *s, double *seconds);
+/* Queues one solve (same arguments as sgdg_batch_add) for nsteps RK4 steps.
+ * t_arrival < 0 means now; a later time holds the request back until then
+ * (submit in arrival order).  y0 is copied. */
+int sgdg_server_submit(sgdg_server *s, int kind, int D, int k, int n, int scheme, const double *a, double dt,
+                       const double *y0, int64_t nsteps, double t_arrival, int64_t *request_id);
+/* One admit / advance / retire round; *completed = requests finished in it.
+ * Synchronises the server's stream. */
+int sgdg_server_tick(sgdg_server *s, int *completed);
+/* State (SGDG_REQ_*), steps done and the three times of a request (-1 where
+ * not reached yet). */
+int sgdg_server_status(sgdg_server *s, int64_t request_id, int *state, int64_t *steps_done, double *t_arrival,
+                       double *t_admit, double *t_done);
+/* Copies a finished request's state (N or 2N values) and forgets the request;
+ * a failed or cancelled request returns its error code instead. */
+int sgdg_server_result(sgdg_server *s, int64_t request_id, double *y);
+/* Removes a queued or running request (its result becomes SGDG_ECANCELLED). */
+int sgdg_server_cancel(sgdg_server *s, int64_t request_id);
+/* Queue length, running requests, finished requests not yet collected, and
+ * DOF-updates (state coefficients x RK stages) executed so far. */
+int sgdg_server_counts(sgdg_server *s, int64_t *queued, int64_t *running, int64_t *finished, double *dof_updates);
+
 /* ---- resources ---------------------------------------------------------- */
 /* Upper bound on device bytes the library may hold (0 = no limit). */
 int sgdg_set_hbm_budget(int64_t bytes);
