@@ -16,8 +16,13 @@ e2e:    the same metric through the C ABI with host buffers: every timed step
         uploads all states from page-locked host memory, advances one RK4
         step and downloads all states.
 plain_fp64: the drop-in form (assembled FP64 CSR SpMV + FP64 RK4) on one solve.
+uneven_batch: 256 advection solves of uneven (D, k, n) in the same launches,
+        with default and with autotuned tile shapes.
 cpu_baseline: the FP64 CPU oracle (OpenMP, all host threads) on a bounded
         sample; it also checks the error of solve 0 against the GPU result.
+serving: a seeded Poisson stream of advection requests of uneven (D, k, n)
+        through the request loop (continuous batching), p50/p99 latency and
+        DOF-updates/s, beside the plain per-request FP64 path (FIFO).
 
 --impl reference times the reference's CPU implementation of the path: the
 Julia package cannot run here (no julia), so its C restatement (oracle/) runs
@@ -52,6 +57,9 @@ def parse():
     p.add_argument("--solves", type=int, default=256)
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--serve-requests", type=int, default=32, help="requests in the serving stream (0: skip)")
+    p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the stream, 1/s")
+    p.add_argument("--serve-chunk", type=int, default=25, help="max RK4 steps between admissions")
     return p.parse_args()
 
 
@@ -160,6 +168,136 @@ def cpu_oracle_leg(y0, gpu_state, steps, nthreads):
     return y0.size * 4.0 * steps / el, el, nthreads, err
 
 
+def timed_steps(b, stream, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        b.step(1)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        b.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def uneven_batch_leg(sg, stream, steps=50, warmup=5):
+    """256 independent advection solves, D in {2,3}, k in {2,3,4}, n in
+    {4..7}, one persistent launch per stage: default tile shapes, then the
+    autotuned ones."""
+    import importlib
+    sv = importlib.import_module(sg.__name__ + ".serving")
+    specs = sv.uneven_batch(256, seed=33)
+    saved = {(d, k): sg.tile_shape(d, k) for d in (2, 3) for k in (2, 3, 4)}
+    sg.clear_tile_shapes()
+    b = sg.Batch()
+    b.set_stream(stream.cuda_stream)
+    for d, k, n, a, modes in specs:
+        b.add("advect", d, k, n, sg.fourier_coeffs(d, k, n, modes), 1e-3, a=a)
+    _, dofs = b.step_info()
+    ms_default = timed_steps(b, stream, steps, warmup)
+    b.autotune()
+    ms_tuned = timed_steps(b, stream, steps, warmup)
+    shapes = {"D%d_k%d" % (d, k): list(sg.tile_shape(d, k)[:2]) for d in (2, 3) for k in (2, 3, 4)}
+    total = b.total_size()
+    b.close()
+    for (d, k), (w, c, tuned) in saved.items():
+        if tuned:
+            sg.set_tile_shape(d, k, w, c)
+    return {"workload": "256 advection solves, D 2-3, k 2-4, n 4-7, dt 1e-3", "state_dofs": int(total),
+            "working_set_bytes": int(28 * total), "steps": steps,
+            "default_tiles": {"value": dofs / (ms_default / 1e3), "ms_per_step": ms_default},
+            "autotuned_tiles": {"value": dofs / (ms_tuned / 1e3), "ms_per_step": ms_tuned},
+            "shapes_wmult_coop": shapes}
+
+
+PLAIN_MEASURE_MAX_N = 1_100_000  # larger plain operators take minutes to assemble on the host
+
+
+def serving_leg(sg, args):
+    """Poisson stream of advection requests of uneven (D, k, n) through the
+    request loop (continuous batching), and the same stream through the plain
+    per-request FP64 path: a single first-in-first-out server whose service
+    time per request is measured on the GPU (assembly of sum_d a_d D_d and the
+    RK4 steps; the D_d of each (D, k, n) are cached, as a serving process
+    would) and replayed against the same arrival times."""
+    import importlib
+    sv = importlib.import_module(sg.__name__ + ".serving")
+    reqs = sv.poisson_stream(sg, args.serve_requests, args.serve_rate, seed=5)
+    y0s = [sv.initial_state(sg, r) for r in reqs]
+    srv = sg.Server(max_chunk_steps=args.serve_chunk)
+    # warm-up: one short request per (k, n) so every 1D table exists before the stream
+    for k, n in sorted({(r.k, r.n) for r in reqs}):
+        N = sg.get_size(2, k, n)
+        srv.submit("advect", 2, k, n, np.zeros(N), 1e-3, 1, a=[1.0, 0.0])
+    while srv.counts()[0] + srv.counts()[1] > 0:
+        srv.tick()
+    srv.close()
+    srv = sg.Server(max_chunk_steps=args.serve_chunk)
+    times, results, dof, makespan = sv.run_stream(sg, srv, reqs, y0s)
+    lat = np.array([t[2] - t[0] for t in times])
+    wait = np.array([t[1] - t[0] for t in times])
+    ok = sum(1 for t in times if t[3] == srv.DONE)
+    srv.close()
+
+    # plain per-request FP64 path: service time per (D, k, n) = fixed + steps x per-step
+    svc_model = {}
+    for r, y0 in zip(reqs, y0s):
+        key = (r.D, r.k, r.n)
+        if key in svc_model or y0.size > PLAIN_MEASURE_MAX_N:
+            continue
+        op = sg.SparseGridOperator(r.D, r.k, r.n)
+        sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, r.dt, nsteps=1, method="plain", op=op)  # builds D_d
+        t = []
+        for ns in (2, 12):
+            t0 = time.perf_counter()
+            sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, ns * r.dt, nsteps=ns, method="plain", op=op)
+            t.append(time.perf_counter() - t0)
+        per = max((t[1] - t[0]) / 10.0, 1e-9)
+        svc_model[key] = (max(t[0] - 2 * per, 0.0), per, y0.size)
+        op.close()
+    # requests too large to assemble here: the measured per-DOF-update rate of the largest measured size
+    big_key = max(svc_model, key=lambda kk: svc_model[kk][2])
+    fixed_b, per_b, n_b = svc_model[big_key]
+    service, extrapolated = [], 0
+    for r, y0 in zip(reqs, y0s):
+        key = (r.D, r.k, r.n)
+        if key in svc_model:
+            fixed, per, _ = svc_model[key]
+        else:
+            fixed, per = fixed_b * y0.size / n_b, per_b * y0.size / n_b
+            extrapolated += 1
+        service.append(fixed + per * r.nsteps)
+    arr = np.array([r.t_arrival for r in reqs])
+    plain_lat = sv.fifo_latencies(arr, service)
+    plain_makespan = float(np.max(arr + plain_lat) - arr[0])
+    total_dof = float(sum(4.0 * y.size * r.nsteps for r, y in zip(reqs, y0s)))
+
+    # accuracy of served results against the plain FP64 path (the smallest requests)
+    errs = []
+    for i in np.argsort([y.size * r.nsteps for r, y in zip(reqs, y0s)])[:4]:
+        r, y0 = reqs[i], y0s[i]
+        _, st = sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, r.nsteps * r.dt, nsteps=r.nsteps, method="plain")
+        errs.append(float(np.linalg.norm(results[i] - st[-1]) / np.linalg.norm(st[-1])))
+
+    return {
+        "workload": "Poisson stream of advection solves, D 2-5, k 2-3, n 4-8, 100-1000 RK4 steps",
+        "requests": len(reqs), "completed": ok, "arrival_rate_per_s": args.serve_rate,
+        "max_chunk_steps": args.serve_chunk, "state_dofs": int(sum(y.size for y in y0s)),
+        "matfree": {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                    "p50_queue_wait_s": float(np.percentile(wait, 50)),
+                    "dof_updates_per_s": dof / makespan, "makespan_s": makespan},
+        "plain_fp64_per_request": {"p50_latency_s": float(np.percentile(plain_lat, 50)),
+                                   "p99_latency_s": float(np.percentile(plain_lat, 99)),
+                                   "dof_updates_per_s": total_dof / plain_makespan, "makespan_s": plain_makespan,
+                                   "service_times": "measured per (D,k,n) on the GPU, FIFO replay of the arrivals",
+                                   "extrapolated_requests": extrapolated},
+        "rel_l2_vs_plain_fp64": {"max": max(errs), "requests": len(errs)},
+    }
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -212,6 +350,9 @@ def run_ours(args):
     b = sg.Batch()
     ids = [b.add("wave", D, K, NLEV, y0, DT) for y0 in states]
     b.set_stream(stream.cuda_stream)
+    sg.clear_tile_shapes()
+    b.autotune()  # tile shape of (D, k) tuned on this batch (no state change)
+    tile = sg.tile_shape(D, K)
     launches_per_step, dofs_per_step = b.step_info()
 
     for _ in range(args.warmup):
@@ -308,6 +449,10 @@ def run_ours(args):
                        "ms_per_step": 1e3 * plain_s / args.steps},
         "clocks": clocks,
     }
+    line["config"]["tile_shape_wmult_coop"] = list(tile[:2])
+    line["uneven_batch"] = uneven_batch_leg(sg, stream)
+    if args.serve_requests > 0:
+        line["serving"] = serving_leg(sg, args)
     if cpu:
         line["cpu_baseline"] = {"value": cpu[0], "unit": UNIT, "cores": cpu[2], "kind": "port",
                                 "sample": "1 solve, %d RK4 steps (%.1f s), FP64 CSR oracle" % (

@@ -454,6 +454,13 @@ class Batch:
         """All live states into host memory at address ``ptr`` (synchronises)."""
         check(lib().sgdg_batch_download(self._h, ctypes.c_void_p(ptr)))
 
+    def autotune(self):
+        """Tunes the tile shape of every (D, k) in the batch not tuned yet;
+        returns how many were tuned."""
+        n = ctypes.c_int()
+        check(lib().sgdg_batch_autotune(self._h, ctypes.byref(n)))
+        return n.value
+
     def step_info(self):
         launches = ctypes.c_int64()
         dofs = ctypes.c_double()
@@ -536,6 +543,21 @@ class Server:
         d = ctypes.c_double()
         check(lib().sgdg_server_counts(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(f), ctypes.byref(d)))
         return q.value, r.value, f.value, d.value
+
+
+def tile_shape(D, k):
+    """(wmult, coop, tuned) of the pencil tiles of (D, k)."""
+    w, c, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(lib().sgdg_tile_shape(D, k, ctypes.byref(w), ctypes.byref(c), ctypes.byref(t)))
+    return w.value, c.value, bool(t.value)
+
+
+def set_tile_shape(D, k, wmult, coop):
+    check(lib().sgdg_set_tile_shape(D, k, wmult, coop))
+
+
+def clear_tile_shapes():
+    check(lib().sgdg_clear_tile_shapes())
 
 
 def set_hbm_budget(nbytes):

@@ -22,7 +22,8 @@ EXPORTS = [
     "sgdg_advect_evolve",
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
-    "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info",
+    "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info", "sgdg_batch_autotune",
+    "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes",
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
     "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
     "sgdg_server_counts",
@@ -92,6 +93,10 @@ def lib(build=True):
     _sig(L, "sgdg_server_cancel", [_vp, _c64])
     _sig(L, "sgdg_server_counts", [_vp, ctypes.POINTER(_c64), ctypes.POINTER(_c64), ctypes.POINTER(_c64),
                                    ctypes.POINTER(_cd)])
+    _sig(L, "sgdg_batch_autotune", [_vp, ctypes.POINTER(_ci)])
+    _sig(L, "sgdg_tile_shape", [_ci, _ci, ctypes.POINTER(_ci), ctypes.POINTER(_ci), ctypes.POINTER(_ci)])
+    _sig(L, "sgdg_set_tile_shape", [_ci, _ci, _ci, _ci])
+    _sig(L, "sgdg_clear_tile_shapes", [])
     _sig(L, "sgdg_batch_create", [ctypes.POINTER(_vp)])
     _sig(L, "sgdg_batch_destroy", [_vp])
     _sig(L, "sgdg_batch_add", [_vp, _ci, _ci, _ci, _ci, _ci, _vp, _cd, _f64p, ctypes.POINTER(_ci)])

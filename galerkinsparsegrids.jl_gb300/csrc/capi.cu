@@ -485,6 +485,36 @@ int sgdg_batch_add(sgdg_batch* b, int kind, int D, int k, int n, int scheme, con
     API_END
 }
 
+int sgdg_batch_autotune(sgdg_batch* b, int* ntuned) {
+    API_BEGIN
+    NEED(b);
+    const auto done = b->eng.autotune();
+    if (ntuned) *ntuned = (int)done.size();
+    API_END
+}
+
+int sgdg_tile_shape(int D, int k, int* wmult, int* coop, int* tuned) {
+    API_BEGIN
+    const MFTile t = mf_tile(D, k);
+    if (wmult) *wmult = t.wmult;
+    if (coop) *coop = t.coop;
+    if (tuned) *tuned = mf_tile_tuned(D, k) ? 1 : 0;
+    API_END
+}
+
+int sgdg_set_tile_shape(int D, int k, int wmult, int coop) {
+    API_BEGIN
+    if (D < 1 || D > 8 || k < 1 || k > 5) throw Error(SGDG_EINVAL, "tile shapes exist for 1 <= D <= 8, 1 <= k <= 5");
+    mf_set_tile(D, k, MFTile{wmult, coop});
+    API_END
+}
+
+int sgdg_clear_tile_shapes(void) {
+    API_BEGIN
+    mf_clear_tiles();
+    API_END
+}
+
 int sgdg_batch_remove(sgdg_batch* b, int id) {
     API_BEGIN
     NEED(b);

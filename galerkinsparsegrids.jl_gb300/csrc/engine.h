@@ -1,6 +1,7 @@
 // engine.h -- device-side data structures shared by the kernels and the host
 // drivers of libsgdg.  Plain C structs: they are copied to device memory as-is.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 
 namespace sgdg {
@@ -37,7 +38,7 @@ struct MFClass {
     float* u[2];
     float* rhs;               // nslots * N
     const double* dt;         // per slot
-    const float* coef;        // per slot, 8 entries: factor on D_d
+    const float* coef;        // per slot, 16 entries: factor on D_d as hi[8], lo[8]
     const int32_t* status;    // per slot, nonzero = skip the RK update
     int32_t N, Ns;
     int32_t D, k, kD, kind, rs;
@@ -70,9 +71,33 @@ struct MFItem {
     int32_t Wv;        // pass: valid columns
     int32_t kd1;       // pass: k^d
     int32_t kDm1;      // pass: k^(D-1)
+    int32_t rlong;     // pass: leading row blocks swept by a whole warp each
 };
 
 constexpr int kMFThreads = 128;
 constexpr int kSpinLimit = 1 << 22;  // polls of a dependency counter before giving up
+
+// Tile shape of the pass tiles of one (D, k), chosen by the autotuner:
+// a tile has cpt * max(1, 128 / nrb) * wmult columns (nrb = row blocks of the
+// pencil), and the row blocks of levels <= lmax - coop are warp-cooperative.
+struct MFTile {
+    int wmult = 1;
+    int coop = 4;
+};
+MFTile mf_tile(int D, int k);                 // tuned shape, or the default
+bool mf_tile_tuned(int D, int k);
+void mf_set_tile(int D, int k, const MFTile& t);
+void mf_clear_tiles();
+
+inline int mf_rlong(int lmax, int coop) { return lmax > coop ? 1 << (lmax - 1 - coop) : 0; }
+// bytes of dynamic shared memory a pass tile of W columns over nrb row blocks needs
+inline size_t mf_tile_smem(int k, int nrb, int W) { return 4 * (3 * (size_t)W + (size_t)k * nrb * W * 2); }
+constexpr size_t kMFTileSmemMax = 64 * 1024;  // wider tiles are narrowed to fit
+// columns of a pass tile (a power of two)
+inline int mf_tile_cols(int k, int cpt, int nrb, int wmult) {
+    int W = cpt * (nrb < kMFThreads ? kMFThreads / nrb : 1) * wmult;
+    while (W > cpt && mf_tile_smem(k, nrb, W) > kMFTileSmemMax) W >>= 1;
+    return W;
+}
 
 }  // namespace sgdg

@@ -223,7 +223,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     cp_async_wait_all();
     __syncthreads();
     const int lwq = lw - (CPT == 4 ? 2 : 1);
-    const int rlong = it.lmax > 4 ? 1 << (it.lmax - 5) : 0;  // row blocks of levels <= lmax - 4
+    const int rlong = it.rlong;  // row blocks of levels <= lmax - coop (tile shape)
     auto store = [&](float* dst, int rb, int jq, float(&o)[K][CPT]) {
 #pragma unroll
         for (int i = 0; i < K; i++) {
@@ -253,7 +253,8 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         if (s < 0) continue;
         const int rb = row / K, i = row - rb * K;
         float* rp = C.rhs + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
-        float v = __ldg(C.coef + s * 8 + it.d) * Z[e];
+        const float z = Z[e];
+        float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
         if (!first) v += __ldcg(rp);
         __stcg(rp, v);
     }

@@ -10,6 +10,7 @@
 // re-captures it.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "mf_engine.h"
 
@@ -214,14 +215,18 @@ void MFEngine::plan() {
         c.u1.alloc(sizeof(float) * ns * c.Ns);
         c.rhs.alloc(sizeof(float) * ns * c.N);
         std::vector<double> dt(ns);
-        std::vector<float> coef((size_t)ns * 8, 0.f);
+        std::vector<float> coef((size_t)ns * 16, 0.f);
         std::vector<int32_t> status(ns, 0);
         for (int sl = 0; sl < ns; sl++) {
             Solve& s = solves_[c.slots[sl]];
             dt[sl] = s.spec.dt;
-            for (int d = 0; d < 8; d++)
-                coef[sl * 8 + d] =
-                    (float)(s.spec.apply || s.spec.kind == MF_KIND_WAVE ? 1.0 : -s.spec.a[d]);
+            for (int d = 0; d < 8; d++) {
+                // factor on D_d as an FP32 (hi, lo) pair: a rounded velocity
+                // would perturb the operator systematically
+                const double f = s.spec.apply || s.spec.kind == MF_KIND_WAVE ? 1.0 : -s.spec.a[d];
+                coef[sl * 16 + d] = (float)f;
+                coef[sl * 16 + 8 + d] = (float)(f - (double)(float)f);
+            }
             status[sl] = s.cancelled ? 1 : 0;
             double* dst = c.y.as<double>() + (size_t)sl * c.Ns;
             if (!s.pending.empty()) {
@@ -316,7 +321,8 @@ void MFEngine::plan() {
 // so when a phase is handed out, its predecessor was handed out a whole
 // wavefront earlier and is normally complete: CTAs rarely wait, while the
 // groups in flight (about one per phase) keep their reused vectors in L2.
-void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
+void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only,
+                           const std::map<std::pair<int, int>, MFTile>* shapes) {
     struct Group {
         std::vector<std::vector<MFItem>> phases;
     };
@@ -326,8 +332,12 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
         ClassArena& c = *classes_[ci];
         const SolveSpec& sp = solves_[c.slots[0]].spec;
         const int D = sp.D, k = sp.k;
-        const bool wave = sp.kind == MF_KIND_WAVE;
         const int cpt = mf_columns_per_thread(k);
+        MFTile tile = mf_tile(D, k);
+        if (shapes) {
+            auto f = shapes->find({D, k});
+            if (f != shapes->end()) tile = f->second;
+        }
         std::vector<int> dims;
         if (sp.apply && sp.apply_dim >= 0)
             dims.push_back(sp.apply_dim);
@@ -352,10 +362,9 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
                 for (size_t pi = 0; pi < c.pencils[d].size(); pi++) {
                     const Pencil& p = c.pencils[d][pi];
                     const int nrb = 1 << (p.lmax - 1);
-                    const int Wp = cpt * std::max(1, kMFThreads / nrb);
+                    const int Wp = mf_tile_cols(k, cpt, nrb, tile.wmult);
                     const int64_t cbeg = (int64_t)s0 * p.R, cend = (int64_t)s1 * p.R;
-                    const size_t sm = 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * 2);
-                    smem = std::max(smem, sm);
+                    smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
                     for (int64_t g0 = cbeg; g0 < cend; g0 += Wp) {
                         MFItem it{};
                         it.type = ITEM_PASS;
@@ -371,12 +380,13 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
                         it.Wv = (int32_t)std::min<int64_t>(Wp, cend - g0);
                         it.kd1 = kd1;
                         it.kDm1 = kDm1;
+                        it.rlong = mf_rlong(p.lmax, tile.coop);
                         list.push_back(it);
                     }
                 }
                 grp.phases.push_back(std::move(list));
             }
-            if (!sp.apply) {
+            if (!sp.apply && !pass_only) {
                 std::vector<MFItem> list;
                 for (int sl = s0; sl < s1; sl++)
                     for (int64_t e0 = 0; e0 < c.Ns; e0 += kRKChunk) {
@@ -422,6 +432,112 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr) {
     smem += (size_t)tb;
     if (smem > 227 * 1024) throw Error(SGDG_EUNSUPPORTED, "operator table and pencil tile exceed shared memory");
     smem_ = smem;
+}
+
+// ------------------------------------------------------------- tiles ----
+static std::mutex g_tile_mu;
+static std::map<std::pair<int, int>, MFTile> g_tiles;
+
+MFTile mf_tile(int D, int k) {
+    std::lock_guard<std::mutex> g(g_tile_mu);
+    auto f = g_tiles.find({D, k});
+    return f == g_tiles.end() ? MFTile{} : f->second;
+}
+
+bool mf_tile_tuned(int D, int k) {
+    std::lock_guard<std::mutex> g(g_tile_mu);
+    return g_tiles.count({D, k}) != 0;
+}
+
+void mf_set_tile(int D, int k, const MFTile& t) {
+    if (t.wmult < 1 || t.wmult > 64 || (t.wmult & (t.wmult - 1)) || t.coop < 1 || t.coop > 30)
+        throw Error(SGDG_EINVAL, "tile shape: wmult must be a power of two in 1..64 and coop in 1..30");
+    std::lock_guard<std::mutex> g(g_tile_mu);
+    g_tiles[{D, k}] = t;
+}
+
+void mf_clear_tiles() {
+    std::lock_guard<std::mutex> g(g_tile_mu);
+    g_tiles.clear();
+}
+
+// For each (D, k) of the live solves without a tuned shape, times the pass
+// tiles of one RK stage of the whole batch (the RK items left out: pass tiles
+// only read the stage input and overwrite the partial sums, so no state
+// changes) for every candidate shape of that (D, k) -- the others at their
+// current shapes -- and keeps the fastest.  A candidate must beat the current
+// shape by 2 % to replace it.
+std::vector<std::pair<int, int>> MFEngine::autotune() {
+    plan();
+    std::vector<std::pair<int, int>> todo, done;
+    for (auto& cp : classes_) {
+        const SolveSpec& sp = solves_[cp->slots[0]].spec;
+        const std::pair<int, int> dk{sp.D, sp.k};
+        if (!mf_tile_tuned(sp.D, sp.k) && std::find(todo.begin(), todo.end(), dk) == todo.end()) todo.push_back(dk);
+    }
+    if (todo.empty()) return done;
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    std::map<std::pair<int, int>, MFTile> shapes;
+    auto time_shapes = [&]() -> float {
+        std::vector<MFItem> items;
+        int nctr = 0;
+        build_items(items, nctr, true, &shapes);
+        DevBuf ti = upload(items, stream_);
+        DevBuf tc(sizeof(int) * (size_t)std::max(nctr, 1));
+        int bps = 0;
+        CK(mf_configure(smem_, &bps));
+        const int grid = std::max(1, bps) * sms;
+        float best = 1e30f;
+        for (int rep = 0; rep < 4; rep++) {
+            CK(cudaEventRecord(e0, stream_));
+            CK(launch_mf_stage(ti.as<MFItem>(), (int)items.size(), classes_d_.as<MFClass>(), tc.as<int>(), nctr, 1, 0,
+                               err_d_.as<int>(), smem_, table_bytes_, grid, stream_));
+            CK(cudaEventRecord(e1, stream_));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep > 0) best = std::min(best, ms);  // the first launch warms up
+        }
+        if (check_error() != SGDG_OK) throw Error(SGDG_ETIMEOUT, "a bounded device wait gave up while tuning");
+        return best;
+    };
+    try {
+        for (auto& dk : todo) {
+            MFTile best = mf_tile(dk.first, dk.second);
+            shapes[dk] = best;
+            float tbest = time_shapes();
+            for (int wmult : {1, 2, 4, 8})
+                for (int coop : {3, 4, 5, 6}) {
+                    const MFTile cand{wmult, coop};
+                    if (cand.wmult == best.wmult && cand.coop == best.coop) continue;
+                    shapes[dk] = cand;
+                    const float t = time_shapes();
+                    if (t < 0.98f * tbest) {
+                        tbest = t;
+                        best = cand;
+                    }
+                }
+            shapes[dk] = best;
+            mf_set_tile(dk.first, dk.second, best);
+            done.push_back(dk);
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        dirty_ = true;
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dirty_ = true;  // rebuild the work list with the tuned shapes
+    drop_graph();
+    plan();
+    return done;
 }
 
 void MFEngine::capture() {

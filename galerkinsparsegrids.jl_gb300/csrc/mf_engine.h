@@ -42,6 +42,9 @@ class MFEngine {
 
     void step(int64_t nsteps);                  // RK4 steps of every live solve (async)
     void flush() { plan(); }                    // applies pending joins and leaves now
+    // tunes the tile shape of every (D, k) of the live solves that has none
+    // yet (process-wide table); returns the (D, k) tuned now
+    std::vector<std::pair<int, int>> autotune();
     void get_state(int id, double* host);       // synchronises
     void set_state(int id, const double* host); // async (pageable memory is staged)
     void upload_all(const double* host);
@@ -83,7 +86,8 @@ class MFEngine {
     };
 
     void plan();
-    void build_items(std::vector<MFItem>& items, int& nctr);
+    void build_items(std::vector<MFItem>& items, int& nctr, bool pass_only = false,
+                     const std::map<std::pair<int, int>, MFTile>* shapes = nullptr);
     const STable& stab(int k, int n);
     void capture();
     void drop_graph();

@@ -126,6 +126,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         else
             dims.push_back(which - 1);
         const int cpt = mf_columns_per_thread(k);
+        const MFTile tile = mf_tile(D, k);
         int kDm1 = 1;
         for (int q = 0; q < D - 1; q++) kDm1 *= k;
         std::vector<int64_t> boff;
@@ -139,8 +140,8 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                 const int32_t pb = (int32_t)boff.size();
                 for (auto o : p.blockoff) boff.push_back(o);
                 const int nrb = 1 << (p.lmax - 1);
-                const int Wp = cpt * std::max(1, kMFThreads / nrb);
-                smem = std::max(smem, 4 * (3 * (size_t)Wp + (size_t)k * nrb * Wp * 2));
+                const int Wp = mf_tile_cols(k, cpt, nrb, tile.wmult);
+                smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
                 for (int64_t g0 = 0; g0 < p.R; g0 += Wp) {
                     MFItem it{};
                     it.type = ITEM_PASS;
@@ -158,6 +159,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                     it.Wv = (int32_t)std::min<int64_t>(Wp, p.R - g0);
                     it.kd1 = kd1;
                     it.kDm1 = kDm1;
+                    it.rlong = mf_rlong(p.lmax, tile.coop);
                     items.push_back(it);
                 }
             }
@@ -185,7 +187,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         const Region r_ent = L.add(sizeof(int32_t) * op->ent.size());
         const Region r_sval = L.add(sizeof(float) * sval.size());
         const Region r_boff = L.add(sizeof(int64_t) * boff.size());
-        const Region r_coef = L.add(sizeof(float) * 8);
+        const Region r_coef = L.add(sizeof(float) * 16);
         const Region r_status = L.add(sizeof(int32_t));
         const Region r_dt = L.add(sizeof(double));
         const Region r_u = L.add(sizeof(float) * (size_t)N);
@@ -224,7 +226,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         c.kD = (int)ix.kD;
         c.kind = wave ? MF_KIND_WAVE : MF_KIND_ADVECT;
         c.rs = rs;
-        const float coef[8] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+        const float coef[16] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int32_t status = 0;
         const double dt = 0.0;
 

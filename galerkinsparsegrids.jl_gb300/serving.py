@@ -63,6 +63,23 @@ def poisson_stream(sg, count, rate, seed=0, D_range=(2, 5), k_choices=(2, 3), n_
     return out
 
 
+def uneven_batch(count, seed, D_range=(2, 3), k_range=(2, 4), n_range=(4, 7), nmodes=3):
+    """Seeded solves of the uneven-batch workload: (D, k, n, velocity, modes)
+    with D, k, n uniform in their ranges, velocity U(-1, 1)^D and nmodes
+    Fourier modes (wave vectors in [1, 3]^D, amplitudes U(-1, 1))."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        D = int(rng.integers(D_range[0], D_range[1] + 1))
+        k = int(rng.integers(k_range[0], k_range[1] + 1))
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        a = rng.uniform(-1, 1, D)
+        modes = [(tuple(int(v) for v in rng.integers(1, 4, D)), float(rng.uniform(-1, 1)),
+                  "sin" if rng.random() < 0.5 else "cos", 0.0) for _ in range(nmodes)]
+        out.append((D, k, n, a, modes))
+    return out
+
+
 def initial_state(sg, r):
     return sg.fourier_coeffs(r.D, r.k, r.n, r.modes)
 

@@ -102,23 +102,39 @@ def test_served_results_equal_alone_and_oracle(sgdg, serving, O):
     assert overlapped >= 2
 
 
+def _max_concurrency(times):
+    ev = sorted([(t[1], 1) for t in times] + [(t[2], -1) for t in times])
+    c = m = 0
+    for _, d in ev:
+        c += d
+        m = max(m, c)
+    return m
+
+
 @pytest.mark.gpu
 def test_budget_makes_requests_wait_not_fail(sgdg, serving):
-    reqs, y0s = _small_stream(sgdg, serving, count=8, seed=12)
+    # eight requests of one size (D=3, k=3, n=5: 7,344 coefficients), so the
+    # budget below holds two of them at a time
+    reqs = serving.poisson_stream(sgdg, 8, rate=50.0, seed=12, D_range=(3, 3), k_choices=(3,), n_range=(5, 5),
+                                  steps_range=(15, 60))
+    y0s = [serving.initial_state(sgdg, r) for r in reqs]
+    # every request arrives at once (speed up the arrival clock)
     free = sgdg.Server(max_chunk_steps=5)
-    _, ref_results, _, _ = serving.run_stream(sgdg, free, reqs, y0s)
+    ftimes, ref_results, _, _ = serving.run_stream(sgdg, free, reqs, y0s, speed=1e6)
     free.close()
     sgdg.sync()
     base = sgdg.hbm_in_use()
-    biggest = max(24 * y.size + 4 * y.size for y in y0s)
-    # room for roughly two requests at a time (plus work lists and tables)
-    sgdg.set_hbm_budget(base + 5 * biggest + (8 << 20))
+    need = 28 * y0s[0].size  # FP64 y, acc + FP32 u[2], rhs per coefficient
+    # room for two requests at a time (tables and work lists take < 64 KB)
+    sgdg.set_hbm_budget(base + int(2.5 * need) + (64 << 10))
     try:
         srv = sgdg.Server(max_chunk_steps=5)
-        times, results, _, _ = serving.run_stream(sgdg, srv, reqs, y0s)
+        times, results, _, _ = serving.run_stream(sgdg, srv, reqs, y0s, speed=1e6)
         assert all(t[3] == srv.DONE for t in times)
         for got, ref in zip(results, ref_results):
             assert np.array_equal(got, ref)
+        assert _max_concurrency(ftimes) == 8
+        assert 1 <= _max_concurrency(times) <= 2
         # a request that cannot fit even alone fails; the server keeps going
         D, k, n = 3, 3, 7
         big = np.zeros(sgdg.get_size(D, k, n))
