@@ -6,7 +6,14 @@ latency statistics reported next to the per-request plain FP64 path.
 Stream parameters follow the serving workload: D in {2..5}, k in {2, 3},
 n in {4..8}, velocities U(-1, 1)^D, 2-4 Fourier modes with integer wave
 vectors in [1, 3]^D and amplitudes U(-1, 1), 100-1000 RK4 steps, dt at a
-fixed fraction of the RK4 stability limit."""
+fixed fraction (cfl / 2.83) of the RK4 stability limit.
+
+Precision note: the FP32 sweeps accumulate each row's products in FP32, and
+the partial sums of a DG derivative cancel (entries grow like 2^n while the
+result stays O(|u|)), so each apply carries a rounding error of ~1e-7 of the
+state; its effect on the solution grows like dt sqrt(steps).  At cfl = 0.5 a
+1000-step request stays near 1e-6 relative to the FP64 path; at cfl = 2 it
+reaches a few 1e-6."""
 import dataclasses
 import functools
 import time
@@ -35,7 +42,7 @@ def spectral_radius_1d(sg, k, n):
     return float(np.linalg.norm(sg.periodic_DLF_matrix(k, n).toarray(), 2))
 
 
-def stable_dt(sg, k, n, a, cfl=2.0):
+def stable_dt(sg, k, n, a, cfl=0.5):
     """dt with |lambda| dt <= cfl for f_t = -sum_d a_d D_d f.  Each D_d acts on
     a line as a leading block of the skew 1D operator, so its norm is at most
     the 1D spectral radius; classical RK4 is stable on the imaginary axis up
@@ -44,7 +51,7 @@ def stable_dt(sg, k, n, a, cfl=2.0):
 
 
 def poisson_stream(sg, count, rate, seed=0, D_range=(2, 5), k_choices=(2, 3), n_range=(4, 8),
-                   steps_range=(100, 1000), modes_range=(2, 4), cfl=2.0):
+                   steps_range=(100, 1000), modes_range=(2, 4), cfl=0.5):
     """``count`` requests with exponential inter-arrival times of mean 1/rate."""
     rng = np.random.default_rng(seed)
     t = 0.0
