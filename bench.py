@@ -18,6 +18,7 @@ e2e:    the same metric through the C ABI with host buffers: every timed step
 plain_fp64: the drop-in form (assembled FP64 CSR SpMV + FP64 RK4) on one solve.
 uneven_batch: 256 advection solves of uneven (D, k, n) in the same launches,
         with default and with autotuned tile shapes.
+vlasov: Vlasov transport in 2x2v phase space (k=2, n=8), FP64 sparse form.
 cpu_baseline: the FP64 CPU oracle (OpenMP, all host threads) on a bounded
         sample; it also checks the error of solve 0 against the GPU result.
 serving: a seeded Poisson stream of advection requests of uneven (D, k, n)
@@ -57,6 +58,7 @@ def parse():
     p.add_argument("--solves", type=int, default=256)
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--vlasov-steps", type=int, default=500, help="RK4 steps of the 2x2v Vlasov leg (0: skip)")
     p.add_argument("--serve-requests", type=int, default=32, help="requests in the serving stream (0: skip)")
     p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the stream, 1/s")
     p.add_argument("--serve-chunk", type=int, default=25, help="max RK4 steps between admissions")
@@ -211,6 +213,39 @@ def uneven_batch_leg(sg, stream, steps=50, warmup=5):
             "default_tiles": {"value": dofs / (ms_default / 1e3), "ms_per_step": ms_default},
             "autotuned_tiles": {"value": dofs / (ms_tuned / 1e3), "ms_per_step": ms_tuned},
             "shapes_wmult_coop": shapes}
+
+
+def vlasov_leg(sg, steps):
+    """Vlasov-type transport in 2x2v phase space (D = 2 space dimensions),
+    sparse k=2, n=8: seeded force E(x) of amplitude 0.1, Maxwellian in v
+    (sigma 0.15) times (1 + 0.05 cos 2 pi x_1); FP64 sparse operators on the
+    GPU (derivatives, nodal transforms, point products), RK4."""
+    import importlib
+    W = importlib.import_module(sg.__name__ + ".workloads")
+    sv = importlib.import_module(sg.__name__ + ".serving")
+    Dx, k, n = 2, 2, 8
+    t0 = time.perf_counter()
+    op = sg.VlasovOperator(Dx, k, n)
+    setup = time.perf_counter() - t0
+    F, f0 = W.vlasov_case(sg, Dx, k, n, seed=11)
+    rho = sv.spectral_radius_1d(sg, k, n)
+    dt = 1.0 / (rho * (Dx * 1.0 + float(np.sum(np.max(np.abs(F), axis=1)))))
+    sg.vlasov_evolve(Dx, k, n, F, f0, 0.0, dt, nsteps=1, op=op)  # warm: device copies, graph
+    t1 = time.perf_counter()
+    sg.vlasov_evolve(Dx, k, n, F, f0, 0.0, dt, nsteps=1, op=op)
+    one = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    _, st = sg.vlasov_evolve(Dx, k, n, F, f0, 0.0, steps * dt, nsteps=steps, op=op)
+    total = time.perf_counter() - t1
+    per_step = max(total - one, 1e-9) / max(steps - 1, 1)
+    nnz = {w: int(op.transform(*w).nnz) for w in [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"),
+                                                   ("nodal", "modal")]}
+    op.close()
+    return {"workload": "Vlasov 2x2v (D=4 phase space), sparse k=2, n=8, RK4", "state_dofs": int(f0.size),
+            "steps": steps, "dt": dt, "form": "FP64 sparse operators (CSR SpMV), graph per RK4 step",
+            "value": f0.size * 4.0 / per_step, "unit": UNIT, "ms_per_step": 1e3 * per_step,
+            "wall_s_end_to_end": total, "host_setup_s": setup, "transform_nnz": nnz,
+            "rel_l2_change_of_f": float(np.linalg.norm(st[-1] - f0) / np.linalg.norm(f0))}
 
 
 PLAIN_MEASURE_MAX_N = 1_100_000  # larger plain operators take minutes to assemble on the host
@@ -451,6 +486,8 @@ def run_ours(args):
     }
     line["config"]["tile_shape_wmult_coop"] = list(tile[:2])
     line["uneven_batch"] = uneven_batch_leg(sg, stream)
+    if args.vlasov_steps > 0:
+        line["vlasov"] = vlasov_leg(sg, args.vlasov_steps)
     if args.serve_requests > 0:
         line["serving"] = serving_leg(sg, args)
     if cpu:

@@ -386,6 +386,127 @@ def energy_func(D, k, n, soln, scheme="sparse", op=None):
     return np.array(times), np.array(energies)
 
 
+# ------------------------------------------------- nodal bases, Vlasov ----
+_TRANSFORMS = {("modal", "nodal"): 0, ("nodal", "points"): 1, ("points", "nodal"): 2, ("nodal", "modal"): 3}
+
+
+def _transform_id(frm, to):
+    if (frm, to) not in _TRANSFORMS:
+        raise ValueError("transforms: modal->nodal, nodal->points, points->nodal, nodal->modal")
+    return _TRANSFORMS[(frm, to)]
+
+
+def transform_1D(k, n, frm, to):
+    """transform_1D(k, n, from, to) (src/1d_nodal_basis.jl:350-414), CSR."""
+    w = _transform_id(frm, to)
+    L = lib()
+    return _csr_from(lambda p: L.sgdg_transform_1d_nnz(k, n, w, p),
+                     lambda a, b, c: L.sgdg_transform_1d_export(k, n, w, a, b, c), k << n)
+
+
+def transform(D, k, n, frm, to, scheme="sparse"):
+    """transform(D, k, n, from, to) (src/multidim_nodal_basis.jl:83-124), CSR."""
+    w = _transform_id(frm, to)
+    sc = _scheme(scheme)
+    L = lib()
+    return _csr_from(lambda p: L.sgdg_transform_nnz(D, k, n, sc, w, p),
+                     lambda a, b, c: L.sgdg_transform_export(D, k, n, sc, w, a, b, c), get_size(D, k, n, scheme))
+
+
+def make_modal2point_matrices(D, k, n):
+    """(m2n, n2p), src/multidim_nodal_basis.jl:127-133 (D = phase-space dimensions)."""
+    return transform(D, k, n, "modal", "nodal"), transform(D, k, n, "nodal", "points")
+
+
+def make_point2modal_matrices(D, k, n):
+    """(p2n, n2m), src/multidim_nodal_basis.jl:135-141."""
+    return transform(D, k, n, "points", "nodal"), transform(D, k, n, "nodal", "modal")
+
+
+def get_one_modal(D, k, n, scheme="sparse"):
+    """Coefficients of f = 1 (src/basic_function_exact_coeffs.jl:5-8)."""
+    out = np.zeros(get_size(D, k, n, scheme))
+    out[0] = 1.0
+    return out
+
+
+def get_xi_modal(D, i, k, n, scheme="sparse"):
+    """Coefficients of f = 2 x_i - 1 (src/basic_function_exact_coeffs.jl:11-17), i 1-based."""
+    one = np.zeros(k << n)
+    one[0] = 1.0
+    xi = np.zeros(k << n)
+    xi[1] = 1.0 / np.sqrt(3.0)
+    return tensor_construct(D, k, n, [xi if d == i else one for d in range(1, D + 1)], scheme)
+
+
+def get_xi_point(D, i, k, n, m2n, n2p):
+    """Point values of 2 x_i - 1 (src/basic_function_exact_coeffs.jl:39-43)."""
+    return n2p @ (m2n @ get_xi_modal(D, i, k, n))
+
+
+class VlasovOperator:
+    """Operators of vlasov_evolve for D space dimensions (phase space x_1..x_D,
+    p_1..p_D on [0,1]^(2D), velocity 2 p_d - 1), k in {2, 3, 5}."""
+
+    def __init__(self, D, k, n, scheme="sparse"):
+        h = ctypes.c_void_p()
+        check(lib().sgdg_vlasov_create(D, k, n, _scheme(scheme), ctypes.byref(h)))
+        self._h = h
+        self.D, self.k, self.n = D, k, n
+        z = ctypes.c_int64()
+        check(lib().sgdg_vlasov_size(self._h, ctypes.byref(z)))
+        self.N = z.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().sgdg_vlasov_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def v_point(self):
+        out = np.zeros(self.D * self.N)
+        check(lib().sgdg_vlasov_v_point(self._h, out))
+        return out.reshape(self.D, self.N)
+
+    def transform(self, frm, to):
+        w = _transform_id(frm, to)
+        L = lib()
+        return _csr_from(lambda p: L.sgdg_vlasov_transform_nnz(self._h, w, p),
+                         lambda a, b, c: L.sgdg_vlasov_transform_export(self._h, w, a, b, c), self.N)
+
+    def _force(self, F_point):
+        F = np.ascontiguousarray(np.asarray(F_point, np.float64).reshape(self.D, self.N)).reshape(-1)
+        return F
+
+    def rhs(self, F_point, f):
+        out = np.zeros(self.N)
+        check(lib().sgdg_vlasov_rhs(self._h, self._force(F_point), np.ascontiguousarray(f, np.float64), out))
+        return out
+
+
+def vlasov_evolve(D, k, n, F_point, f0_modal, time0, time1, nout=2, order="rk4", scheme="sparse", dt=None,
+                  nsteps=None, op=None):
+    """vlasov_evolve (src/pdes.jl:131-227) with classical RK4 and fixed steps:
+    df/dt = -(v . grad_x f) + F . grad_p f, products taken in the point basis.
+    ``F_point`` holds D arrays of point values.  Returns (times, states)."""
+    _order(order)
+    op = op or VlasovOperator(D, k, n, scheme)
+    f0 = np.ascontiguousarray(f0_modal, np.float64)
+    if f0.shape != (op.N,):
+        raise ValueError("f0 must have %d entries" % op.N)
+    ns = _steps(time0, time1, dt, nsteps)
+    times = np.zeros(nout)
+    states = np.zeros((nout, op.N))
+    check(lib().sgdg_vlasov_evolve(op._h, op._force(F_point), f0, float(time0), float(time1), ns, int(nout), times,
+                                   states.reshape(-1)))
+    return times, list(states)
+
+
 # --------------------------------------------------------------- batches ----
 class Batch:
     """Independent solves of uneven (D, k, n) advanced together by the

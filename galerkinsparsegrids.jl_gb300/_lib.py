@@ -24,6 +24,9 @@ EXPORTS = [
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
     "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info", "sgdg_batch_autotune",
     "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes",
+    "sgdg_transform_1d_nnz", "sgdg_transform_1d_export", "sgdg_transform_nnz", "sgdg_transform_export",
+    "sgdg_vlasov_create", "sgdg_vlasov_destroy", "sgdg_vlasov_size", "sgdg_vlasov_v_point",
+    "sgdg_vlasov_transform_nnz", "sgdg_vlasov_transform_export", "sgdg_vlasov_rhs", "sgdg_vlasov_evolve",
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
     "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
     "sgdg_server_counts",
@@ -81,6 +84,18 @@ def lib(build=True):
     _sig(L, "sgdg_apply_noalloc", [_ci, _ci, _ci, _ci, _ci, _vp, _vp, _vp])
     _sig(L, "sgdg_wave_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
     _sig(L, "sgdg_advect_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
+    _sig(L, "sgdg_transform_1d_nnz", [_ci, _ci, _ci, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_transform_1d_export", [_ci, _ci, _ci, _i64p, _i32p, _f64p])
+    _sig(L, "sgdg_transform_nnz", [_ci, _ci, _ci, _ci, _ci, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_transform_export", [_ci, _ci, _ci, _ci, _ci, _i64p, _i32p, _f64p])
+    _sig(L, "sgdg_vlasov_create", [_ci, _ci, _ci, _ci, ctypes.POINTER(_vp)])
+    _sig(L, "sgdg_vlasov_destroy", [_vp])
+    _sig(L, "sgdg_vlasov_size", [_vp, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_vlasov_v_point", [_vp, _f64p])
+    _sig(L, "sgdg_vlasov_transform_nnz", [_vp, _ci, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_vlasov_transform_export", [_vp, _ci, _i64p, _i32p, _f64p])
+    _sig(L, "sgdg_vlasov_rhs", [_vp, _f64p, _f64p, _f64p])
+    _sig(L, "sgdg_vlasov_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _f64p, _f64p])
     _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_server_destroy", [_vp])
     _sig(L, "sgdg_server_set_stream", [_vp, _vp])

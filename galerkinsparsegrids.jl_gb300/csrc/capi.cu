@@ -21,6 +21,8 @@ namespace sgdg {
 cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st);
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
                            int stage, cudaStream_t st);
+cudaError_t launch_vlasov_combine(const double* w, const double* p, const double* acc_in, const double* other,
+                                  double* out, int64_t n, cudaStream_t st);
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -99,6 +101,64 @@ struct sgdg_op {
     }
 };
 
+// ----------------------------------------------------------- Vlasov ----
+// Operators of vlasov_evolve (src/pdes.jl:131-227) for D space dimensions:
+// phase space of P = 2D dimensions (x_1..x_D, p_1..p_D), grad_matrix(P), the
+// four nodal transforms and the velocity points v_d = n2p m2n (2 p_d - 1).
+struct sgdg_vlasov {
+    int D = 0, P = 0, k = 0, n = 0;
+    SparseIndex ix;
+    std::vector<CSR> Ds;
+    CSR T[4];  // m2n, n2p, p2n, n2m
+    std::vector<double> v_point;  // D x N
+    std::vector<std::unique_ptr<DeviceCSR>> dDs;
+    std::unique_ptr<DeviceCSR> dT[4];
+    DevBuf vpt, F, t, s, p, c1, c2, z;
+    cudaStream_t stream = nullptr;
+    ~sgdg_vlasov() {
+        if (stream) cudaStreamDestroy(stream);
+    }
+    void to_gpu() {
+        if (stream) return;
+        require_gpu();
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        for (auto& A : Ds) dDs.push_back(to_device(A, stream));
+        for (int w = 0; w < 4; w++) dT[w] = to_device(T[w], stream);
+        vpt = upload(v_point, stream);
+        const size_t b = sizeof(double) * (size_t)ix.N;
+        F.alloc(b * D);
+        t.alloc(b);
+        s.alloc(b);
+        p.alloc(b);
+        c1.alloc(b);
+        c2.alloc(b);
+        z.alloc(b);
+    }
+    // z = p2n (-sum_d v_d .* n2p m2n Dx_d u + sum_d F_d .* n2p m2n Dp_d u)
+    cudaError_t rhs_points(const double* u) {
+        const int64_t N = ix.N;
+        const double* vp = vpt.as<double>();
+        const double* Fp = F.as<double>();
+        double *tt = t.as<double>(), *ss = s.as<double>(), *pp = p.as<double>();
+        double *a1 = c1.as<double>(), *a2 = c2.as<double>(), *zz = z.as<double>();
+        cudaError_t e = cudaSuccess;
+        for (int d = 0; d < P && e == cudaSuccess; d++) {
+            e = launch_csr_spmv(dDs[d]->d, u, tt, stream);
+            if (e == cudaSuccess) e = launch_csr_spmv(dT[0]->d, tt, ss, stream);
+            if (e == cudaSuccess) e = launch_csr_spmv(dT[1]->d, ss, pp, stream);
+            if (e != cudaSuccess) break;
+            if (d < D)  // contrib1 = sum_d v_d .* x_d
+                e = launch_vlasov_combine(vp + (size_t)d * N, pp, d == 0 ? nullptr : a1, nullptr, a1, N, stream);
+            else if (d < P - 1)  // contrib2 = sum_d F_d .* p_d
+                e = launch_vlasov_combine(Fp + (size_t)(d - D) * N, pp, d == D ? nullptr : a2, nullptr, a2, N, stream);
+            else  // -contrib1 + contrib2
+                e = launch_vlasov_combine(Fp + (size_t)(d - D) * N, pp, d == D ? nullptr : a2, a1, a2, N, stream);
+        }
+        if (e == cudaSuccess) e = launch_csr_spmv(dT[2]->d, a2, zz, stream);
+        return e;
+    }
+};
+
 struct sgdg_batch {
     MFEngine eng;  // its destructor frees device memory only, never touches a stream
     cudaStream_t own = nullptr;
@@ -120,7 +180,23 @@ static cudaStream_t op_stream(sgdg_op* op) {
     return op->stream;
 }
 
+// nodal transforms: the D-dimensional restricted Kronecker product of a 1D map
+static CSR build_transform(int D, int k, int n, int scheme, int which) {
+    if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
+    return transform_dd(make_index(D, k, n, scheme), transform_1d(k, n, which));
+}
+
+static void export_csr(const CSR& A, int64_t* rowptr, int32_t* col, double* val) {
+    std::memcpy(rowptr, A.rowptr.data(), sizeof(int64_t) * A.rowptr.size());
+    if (A.nnz()) {
+        std::memcpy(col, A.col.data(), sizeof(int32_t) * A.col.size());
+        std::memcpy(val, A.val.data(), sizeof(double) * A.val.size());
+    }
+}
+
 extern "C" {
+
+// ---------------------------------------------------- nodal transforms ----
 
 int sgdg_version(char* buf, size_t len) {
     copy_str("sgdg 0.1 (sm_103a)", buf, len);
@@ -441,6 +517,187 @@ int sgdg_advect_evolve(sgdg_op* op, const double* a, const double* f0, double t0
     } else {
         throw Error(SGDG_EINVAL, "method must be PLAIN (0) or MATFREE (1)");
     }
+    API_END
+}
+
+int sgdg_transform_1d_nnz(int k, int n, int which, int64_t* nnz) {
+    API_BEGIN
+    NEED(nnz);
+    *nnz = transform_1d(k, n, which).nnz();
+    API_END
+}
+
+int sgdg_transform_1d_export(int k, int n, int which, int64_t* rowptr, int32_t* col, double* val) {
+    API_BEGIN
+    NEED(rowptr);
+    export_csr(transform_1d(k, n, which), rowptr, col, val);
+    API_END
+}
+
+int sgdg_transform_nnz(int D, int k, int n, int scheme, int which, int64_t* nnz) {
+    API_BEGIN
+    NEED(nnz);
+    *nnz = build_transform(D, k, n, scheme, which).nnz();
+    API_END
+}
+
+int sgdg_transform_export(int D, int k, int n, int scheme, int which, int64_t* rowptr, int32_t* col, double* val) {
+    API_BEGIN
+    NEED(rowptr);
+    export_csr(build_transform(D, k, n, scheme, which), rowptr, col, val);
+    API_END
+}
+
+// ------------------------------------------------------------- Vlasov ----
+int sgdg_vlasov_create(int D, int k, int n, int scheme, sgdg_vlasov** out) {
+    API_BEGIN
+    NEED(out);
+    if (D < 1 || 2 * D > 8) throw Error(SGDG_EINVAL, "D (space dimensions) must be 1..4");
+    if (k != 2 && k != 3 && k != 5) throw Error(SGDG_EINVAL, "the nodal basis exists for k = 2, 3, 5");
+    auto v = std::make_unique<sgdg_vlasov>();
+    v->D = D;
+    v->P = 2 * D;
+    v->k = k;
+    v->n = n;
+    v->ix = make_index(v->P, k, n, scheme);
+    auto dlf = dlf1d(k, n);
+    for (int d = 0; d < v->P; d++) v->Ds.push_back(assemble_dd(v->ix, *dlf, d));
+    for (int w = 0; w < 4; w++) v->T[w] = transform_dd(v->ix, transform_1d(k, n, w));
+    // v_modal_d = tensor product of 1 (coefficient 1 on the first block) and,
+    // along p_d, 2 p_d - 1 (coefficient 1/sqrt(3) on mode 2), src/pdes.jl:166-172
+    const int64_t N = v->ix.N;
+    v->v_point.assign((size_t)D * N, 0.0);
+    std::vector<double> vm(N, 0.0), tmp(N, 0.0);
+    for (int d = 0; d < D; d++) {
+        std::fill(vm.begin(), vm.end(), 0.0);
+        // level (1..1), cell (1..1), mode 1 except mode 2 along dimension D + d
+        vm[(size_t)std::pow((double)k, (double)(D + d))] = 1.0 / std::sqrt(3.0);
+        // m2n then n2p on the host
+        auto spmv = [&](const CSR& A, const std::vector<double>& x, std::vector<double>& y) {
+            for (int64_t i = 0; i < A.m; i++) {
+                double acc = 0.0;
+                for (int64_t q = A.rowptr[i]; q < A.rowptr[i + 1]; q++) acc += A.val[q] * x[A.col[q]];
+                y[i] = acc;
+            }
+        };
+        spmv(v->T[0], vm, tmp);
+        std::vector<double> pt(N);
+        spmv(v->T[1], tmp, pt);
+        std::copy(pt.begin(), pt.end(), v->v_point.begin() + (size_t)d * N);
+    }
+    *out = v.release();
+    API_END
+}
+
+int sgdg_vlasov_destroy(sgdg_vlasov* v) {
+    API_BEGIN
+    delete v;
+    API_END
+}
+
+int sgdg_vlasov_size(const sgdg_vlasov* v, int64_t* N) {
+    API_BEGIN
+    NEED(v);
+    NEED(N);
+    *N = v->ix.N;
+    API_END
+}
+
+int sgdg_vlasov_v_point(const sgdg_vlasov* v, double* out) {
+    API_BEGIN
+    NEED(v);
+    NEED(out);
+    std::copy(v->v_point.begin(), v->v_point.end(), out);
+    API_END
+}
+
+int sgdg_vlasov_transform_nnz(const sgdg_vlasov* v, int which, int64_t* nnz) {
+    API_BEGIN
+    NEED(v);
+    NEED(nnz);
+    if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
+    *nnz = v->T[which].nnz();
+    API_END
+}
+
+int sgdg_vlasov_transform_export(const sgdg_vlasov* v, int which, int64_t* rowptr, int32_t* col, double* val) {
+    API_BEGIN
+    NEED(v);
+    NEED(rowptr);
+    if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
+    export_csr(v->T[which], rowptr, col, val);
+    API_END
+}
+
+int sgdg_vlasov_rhs(sgdg_vlasov* v, const double* F_point, const double* f, double* out) {
+    API_BEGIN
+    NEED(v);
+    NEED(F_point);
+    NEED(f);
+    NEED(out);
+    v->to_gpu();
+    const int64_t N = v->ix.N;
+    const size_t b = sizeof(double) * (size_t)N;
+    DevBuf u(b), r(b);
+    CK(cudaMemcpyAsync(v->F.p, F_point, b * v->D, cudaMemcpyHostToDevice, v->stream));
+    CK(cudaMemcpyAsync(u.p, f, b, cudaMemcpyHostToDevice, v->stream));
+    CK(v->rhs_points(u.as<double>()));
+    CK(launch_csr_spmv(v->dT[3]->d, v->z.as<double>(), r.as<double>(), v->stream));
+    CK(cudaMemcpyAsync(out, r.p, b, cudaMemcpyDeviceToHost, v->stream));
+    CK(cudaStreamSynchronize(v->stream));
+    API_END
+}
+
+int sgdg_vlasov_evolve(sgdg_vlasov* v, const double* F_point, const double* f0, double t0, double t1, int64_t nsteps,
+                       int nout, double* times, double* states) {
+    API_BEGIN
+    NEED(v);
+    NEED(F_point);
+    NEED(f0);
+    NEED(states);
+    check_evolve_args(nsteps, nout, t0, t1);
+    v->to_gpu();
+    cudaStream_t st = v->stream;
+    const int64_t N = v->ix.N;
+    const size_t b = sizeof(double) * (size_t)N;
+    DevBuf y(b), acc(b), u0(b), u1(b);
+    CK(cudaMemcpyAsync(v->F.p, F_point, b * v->D, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(y.p, f0, b, cudaMemcpyHostToDevice, st));
+    const double dt = (t1 - t0) / double(nsteps);
+    // one RK4 step as a graph: per stage the right-hand side in the point
+    // basis, then n2m fused with the stage update
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const double* in[4] = {y.as<double>(), u0.as<double>(), u1.as<double>(), u0.as<double>()};
+    double* outv[4] = {u0.as<double>(), u1.as<double>(), u0.as<double>(), u1.as<double>()};
+    cudaError_t e = cudaSuccess;
+    for (int stage = 1; stage <= 4 && e == cudaSuccess; stage++) {
+        e = v->rhs_points(in[stage - 1]);
+        if (e == cudaSuccess)
+            e = launch_csr_rk4(v->dT[3]->d, v->z.as<double>(), y.as<double>(), acc.as<double>(), outv[stage - 1], dt,
+                               stage, st);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        throw Error(SGDG_ECUDA, std::string("capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) throw Error(SGDG_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e3));
+    auto steps = out_steps(nsteps, nout);
+    int64_t done = 0;
+    cudaError_t err = cudaSuccess;
+    for (int i = 0; i < nout && err == cudaSuccess; i++) {
+        for (; done < steps[i] && err == cudaSuccess; done++) err = cudaGraphLaunch(ge, st);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(states + (size_t)i * N, y.p, b, cudaMemcpyDeviceToHost, st);
+        if (times) times[i] = t0 + (t1 - t0) * double(steps[i]) / double(nsteps);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    cudaGraphExecDestroy(ge);
+    if (err != cudaSuccess) throw Error(SGDG_ECUDA, std::string("vlasov evolve: ") + cudaGetErrorString(err));
     API_END
 }
 

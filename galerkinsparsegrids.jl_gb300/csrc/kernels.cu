@@ -61,6 +61,17 @@ __global__ void k_f32_to_f64(const float* __restrict__ a, double* __restrict__ b
         b[i] = (double)a[i];
 }
 
+// Vlasov right-hand side in the point basis (src/pdes.jl:185-191):
+//   acc_out = (acc_in or 0) + w .* p; with `other` set, out = -other + acc_out.
+__global__ void k_vlasov_combine(const double* __restrict__ w, const double* __restrict__ p, const double* acc_in,
+                                 const double* __restrict__ other, double* out, int64_t n) {  // out may be acc_in
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double prod = w[i] * p[i];
+        const double a = acc_in ? acc_in[i] + prod : prod;
+        out[i] = other ? -other[i] + a : a;
+    }
+}
+
 // ------------------------------------------------------------ launchers ----
 static int grid_for(int64_t threads) {
     int64_t b = (threads + 255) / 256;
@@ -106,4 +117,13 @@ cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t
     return cudaGetLastError();
 }
 
+}  // namespace sgdg
+
+namespace sgdg {
+cudaError_t launch_vlasov_combine(const double* w, const double* p, const double* acc_in, const double* other,
+                                  double* out, int64_t n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_vlasov_combine<<<grid_for(n) > 4096 ? 4096 : grid_for(n), 256, 0, st>>>(w, p, acc_in, other, out, n);
+    return cudaGetLastError();
+}
 }  // namespace sgdg

@@ -117,6 +117,18 @@ CSR spgemm_sum(const std::vector<const CSR*>& A);                  // sum_i A_i 
 CSR add_scaled(const std::vector<const CSR*>& A, const std::vector<double>& s);
 CSR wave_rhs(const CSR& lap);                                                // wave_data
 
+// ------------------------------------------------------ nodal transforms ----
+// Maps between the modal (hierarchical), nodal and point bases of the Vlasov
+// evolver (src/1d_nodal_basis.jl, src/multidim_nodal_basis.jl), k in {2,3,5}.
+enum : int {
+    TRANSFORM_MODAL_TO_NODAL = 0,
+    TRANSFORM_NODAL_TO_POINTS = 1,
+    TRANSFORM_POINTS_TO_NODAL = 2,
+    TRANSFORM_NODAL_TO_MODAL = 3
+};
+CSR transform_1d(int k, int n, int which);                  // transform_1D
+CSR transform_dd(const SparseIndex& ix, const CSR& T1);      // transform(D, k, n, mat_1D)
+
 // ------------------------------------------------------ pencil schedule ----
 // A pencil for dimension d fixes the levels of every other dimension; its
 // elements are whole level blocks (L_-d, l) for l = 1..Lmax and form an

@@ -119,6 +119,38 @@ int sgdg_wave_evolve(sgdg_op *op, const double *f0, const double *v0, double t0,
 int sgdg_advect_evolve(sgdg_op *op, const double *a, const double *f0, double t0, double t1, int64_t nsteps,
                        int nout, int method, double *times, double *states);
 
+/* ---- nodal bases and the Vlasov evolver ---------------------------------- */
+/* Basis maps of the Vlasov evolver (k = 2, 3 or 5):
+ * which 0 modal -> nodal, 1 nodal -> points, 2 points -> nodal, 3 nodal -> modal.
+ * transform_1D(k, n, from, to) (src/1d_nodal_basis.jl:350-414), k 2^n square CSR. */
+int sgdg_transform_1d_nnz(int k, int n, int which, int64_t *nnz);
+int sgdg_transform_1d_export(int k, int n, int which, int64_t *rowptr, int32_t *col, double *val);
+/* transform(D, k, n, from, to) (src/multidim_nodal_basis.jl:83-124): the 1D map
+ * tensored over D dimensions on the sparse grid, CSR (N x N). */
+int sgdg_transform_nnz(int D, int k, int n, int scheme, int which, int64_t *nnz);
+int sgdg_transform_export(int D, int k, int n, int scheme, int which, int64_t *rowptr, int32_t *col, double *val);
+
+/* vlasov_evolve (src/pdes.jl:131-227) for D space dimensions: phase space of
+ * 2D dimensions ordered x_1..x_D, p_1..p_D, velocity v_d = 2 p_d - 1.  The
+ * handle builds what the reference takes as arguments or builds inside:
+ * grad_matrix(2D, k, n), m2n, n2p, p2n, n2m and v_point. */
+typedef struct sgdg_vlasov sgdg_vlasov;
+int sgdg_vlasov_create(int D, int k, int n, int scheme, sgdg_vlasov **out);
+int sgdg_vlasov_destroy(sgdg_vlasov *v);
+int sgdg_vlasov_size(const sgdg_vlasov *v, int64_t *N);
+/* v_point (D x N, point basis), src/pdes.jl:166-172 */
+int sgdg_vlasov_v_point(const sgdg_vlasov *v, double *out);
+/* the transforms held by the handle (which as above), CSR */
+int sgdg_vlasov_transform_nnz(const sgdg_vlasov *v, int which, int64_t *nnz);
+int sgdg_vlasov_transform_export(const sgdg_vlasov *v, int which, int64_t *rowptr, int32_t *col, double *val);
+/* steprule (src/pdes.jl:174-192): out = df/dt for the modal state f and the
+ * force F_point (D x N, point basis), FP64 on the GPU. */
+int sgdg_vlasov_rhs(sgdg_vlasov *v, const double *F_point, const double *f, double *out);
+/* Classical RK4 with nsteps fixed steps on [t0, t1]; nout >= 2 equally spaced
+ * states (the first is f0), FP64 sparse operators on the GPU. */
+int sgdg_vlasov_evolve(sgdg_vlasov *v, const double *F_point, const double *f0, double t0, double t1, int64_t nsteps,
+                       int nout, double *times, double *states);
+
 /* ---- batches of independent solves (matrix-free form) ------------------- */
 /* Many solves of uneven D, k, n advance together: each RK stage is one
  * persistent launch over the pencil tiles and RK chunks of every solve, and

@@ -78,6 +78,10 @@ def lib():
         L.or_fourier_coeffs.argtypes = [ctypes.c_int] * 5 + [_i32p, _f64p, _i32p, _f64p, _f64p]
         L.or_tensor_construct.argtypes = [ctypes.c_int] * 4 + [_f64p, _f64p]
         L.or_reconstruct.argtypes = [ctypes.c_int] * 4 + [_f64p, ctypes.c_int64, _f64p, _f64p]
+        L.or_transform_1d.argtypes = [ctypes.c_int] * 3
+        L.or_transform_1d.restype = vp
+        L.or_transform.argtypes = [ctypes.c_int] * 4 + [vp]
+        L.or_transform.restype = vp
         L.or_cell_index.argtypes = [ctypes.c_double, ctypes.c_int]
         L.or_cell_index.restype = ctypes.c_int
         L.or_init()
@@ -321,3 +325,75 @@ def energy(D, k, n, state, scheme="sparse", grads=None):
     grads = grads if grads is not None else grad_matrix(D, k, n, scheme)
     u, ut = state[:N], state[N:]
     return sum(float(np.sum((G @ u) ** 2)) for G in grads) + float(np.sum(ut ** 2))
+
+
+# ------------------------------------------------------- nodal transforms ----
+TRANSFORMS = {("modal", "nodal"): 0, ("nodal", "points"): 1, ("points", "nodal"): 2, ("nodal", "modal"): 3}
+
+
+def transform_1D(k, n, frm, to):
+    """transform_1D (src/1d_nodal_basis.jl:350-414) for the four maps of the
+    Vlasov evolver, CSC."""
+    return _Mat(lib().or_transform_1d(k, n, TRANSFORMS[(frm, to)])).csc()
+
+
+def transform(D, k, n, frm, to, scheme="sparse"):
+    """transform(D, k, n, from, to) (src/multidim_nodal_basis.jl:83-124),
+    assembled like the reference (restricted Kronecker product), CSC."""
+    T1 = _Mat(lib().or_transform_1d(k, n, TRANSFORMS[(frm, to)]))
+    return _Mat(lib().or_transform(D, k, n, _scheme(scheme), T1.ptr)).csc()
+
+
+def get_one_modal(D, k, n, scheme="sparse"):
+    """src/basic_function_exact_coeffs.jl:5-8"""
+    out = np.zeros(get_size(D, k, n, scheme))
+    out[0] = 1.0
+    return out
+
+
+def get_xi_modal(D, i, k, n, scheme="sparse"):
+    """src/basic_function_exact_coeffs.jl:11-17: coefficients of 2 x_i - 1."""
+    one = np.zeros(k << n)
+    one[0] = 1.0
+    xi = np.zeros(k << n)
+    xi[1] = 1.0 / np.sqrt(3.0)
+    return tensor_construct(D, k, n, [xi if d == i else one for d in range(1, D + 1)], scheme)
+
+
+def vlasov_rhs(D, k, n, ops, F_point, f):
+    """steprule of vlasov_evolve (src/pdes.jl:174-192) with assembled
+    operators ``ops`` = (Ds (2D CSR), m2n, n2p, p2n, n2m) and the velocity
+    points v_point built as in src/pdes.jl:166-172."""
+    Ds, m2n, n2p, p2n, n2m, v_point = ops
+    dfdx = [Ds[d] @ f for d in range(D)]
+    dfdp = [Ds[d] @ f for d in range(D, 2 * D)]
+    xpt = [n2p @ (m2n @ x) for x in dfdx]
+    ppt = [n2p @ (m2n @ x) for x in dfdp]
+    c1 = sum(v_point[d] * xpt[d] for d in range(D))
+    c2 = sum(F_point[d] * ppt[d] for d in range(D))
+    return n2m @ (p2n @ (-c1 + c2))
+
+
+def vlasov_operators(D, k, n, scheme="sparse"):
+    """Assembled operators of vlasov_evolve for D space dimensions (2D-dim
+    phase space): grad_matrix(2D), the four transforms and v_point."""
+    P = 2 * D
+    Ds = [D_matrix(P, d, k, n, scheme).tocsr() for d in range(1, P + 1)]
+    m2n = transform(P, k, n, "modal", "nodal", scheme).tocsr()
+    n2p = transform(P, k, n, "nodal", "points", scheme).tocsr()
+    p2n = transform(P, k, n, "points", "nodal", scheme).tocsr()
+    n2m = transform(P, k, n, "nodal", "modal", scheme).tocsr()
+    v_point = [n2p @ (m2n @ get_xi_modal(P, D + d, k, n, scheme)) for d in range(1, D + 1)]
+    return Ds, m2n, n2p, p2n, n2m, v_point
+
+
+def vlasov_rk4(D, k, n, ops, F_point, f0, dt, nsteps):
+    """Classical RK4 on the Vlasov right-hand side (FP64)."""
+    y = np.array(f0, np.float64)
+    for _ in range(nsteps):
+        k1 = vlasov_rhs(D, k, n, ops, F_point, y)
+        k2 = vlasov_rhs(D, k, n, ops, F_point, y + 0.5 * dt * k1)
+        k3 = vlasov_rhs(D, k, n, ops, F_point, y + 0.5 * dt * k2)
+        k4 = vlasov_rhs(D, k, n, ops, F_point, y + dt * k3)
+        y = y + (dt / 6.0) * (k1 + 2.0 * k2 + 2.0 * k3 + k4)
+    return y

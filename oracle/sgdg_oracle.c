@@ -1133,3 +1133,326 @@ int or_cell_index(double x, int l) {
     if (x >= 1) return 1 << (l - 1);
     return 1 + (int)floor((double)(1 << (l - 1)) * x);
 }
+
+/* ------------------------------------------------------------------------- */
+/* Nodal basis and basis transforms: src/1d_nodal_basis.jl,                  */
+/* src/multidim_nodal_basis.jl                                               */
+/* ------------------------------------------------------------------------- */
+
+/* lag_nodal, src/1d_nodal_basis.jl:46-66 (k in {2, 3, 5}) */
+static double lag_nodal(int k, int mode, double x) {
+    if (x < 0 || x > 1) return 0.0;
+    if (k == 2) return mode == 1 ? x : 1 - x;
+    if (k == 3) {
+        if (mode == 1) return 2 * (x - 0.5) * (x - 1);
+        if (mode == 2) return -4 * x * (x - 1);
+        return 2 * x * (x - 0.5);
+    }
+    /* k == 5 */
+    if (mode == 1) return 32.0 / 3 * (x - 0.25) * (x - 0.5) * (x - 0.75) * (x - 1);
+    if (mode == 2) return -128.0 / 3 * x * (x - 0.5) * (x - 0.75) * (x - 1);
+    if (mode == 3) return 64 * x * (x - 0.25) * (x - 0.75) * (x - 1);
+    if (mode == 4) return -128.0 / 3 * x * (x - 0.25) * (x - 0.5) * (x - 1);
+    return 32.0 / 3 * x * (x - 0.25) * (x - 0.5) * (x - 0.75);
+}
+
+/* h_nodal, src/1d_nodal_basis.jl:69-99 */
+static double h_nodal(int k, int mode, double x) {
+    if (k == 2) {
+        if (mode == 1) return fmax(0.0, 1 - fabs(x));
+        if (fabs(x) > 1 || x == 0) return 0.0;
+        return x < 0 ? x + 1 : 0.0;
+    }
+    if (k == 3) {
+        if (mode == 1) return fmax(0.0, -4 * x * (x + 1));
+        if (mode == 2) return fmax(0.0, -4 * x * (x - 1));
+        if (fabs(x) > 1 || x == 0) return 0.0;
+        return x < 0 ? 2 * (x + 1) * (x + 0.5) : 0.0;
+    }
+    /* k == 5 */
+    if (mode == 1) return (x < -1 || x > 0) ? 0.0 : -128.0 / 3 * x * (x + 1) * (x + 0.5) * (x + 0.25);
+    if (mode == 2) return (x < -1 || x > 0) ? 0.0 : -128.0 / 3 * x * (x + 1) * (x + 0.5) * (x + 0.75);
+    if (mode == 3) return (x > 1 || x < 0) ? 0.0 : -128.0 / 3 * x * (x - 1) * (x - 0.5) * (x - 0.75);
+    if (mode == 4) return (x > 1 || x < 0) ? 0.0 : -128.0 / 3 * x * (x - 1) * (x - 0.5) * (x - 0.25);
+    if (fabs(x) > 1 || x == 0) return 0.0;
+    return x < 0 ? 32.0 / 3 * (x + 1) * (x + 0.75) * (x + 0.5) * (x + 0.25) : 0.0;
+}
+
+/* v_nodal, src/1d_nodal_basis.jl:102-108 */
+static double v_nodal(int k, int level, int cell, int mode, double x) {
+    if (level == 0) return lag_nodal(k, mode, x);
+    return h_nodal(k, mode, (double)(1 << level) * x - (2 * cell - 1));
+}
+
+/* threshold(sparse, atol), src/additional_tools.jl:34-42: |v| < atol -> dropped */
+static or_mat *mat_threshold(const or_mat *A, double atol) {
+    or_mat *B = mat_alloc(A->m, A->n, A->nnz);
+    int64_t w = 0;
+    for (int64_t j = 0; j < A->n; j++) {
+        B->colptr[j] = w;
+        for (int64_t p = A->colptr[j]; p < A->colptr[j + 1]; p++)
+            if (!(fabs(A->nzval[p]) < atol) && A->nzval[p] != 0) {
+                B->rowval[w] = A->rowval[p];
+                B->nzval[w] = A->nzval[p];
+                w++;
+            }
+    }
+    B->colptr[A->n] = w;
+    B->nnz = w;
+    return B;
+}
+
+/* threshold(inv(Matrix(A)), atol): Gauss-Jordan with partial pivoting on the
+ * dense copy (LAPACK's getrf/getri in Julia; values agree to roundoff). */
+static or_mat *mat_inverse_threshold(const or_mat *A, double atol) {
+    int64_t n = A->n;
+    double *M = calloc((size_t)(n * 2 * n), sizeof(double));
+    for (int64_t j = 0; j < n; j++)
+        for (int64_t p = A->colptr[j]; p < A->colptr[j + 1]; p++) M[A->rowval[p] * 2 * n + j] = A->nzval[p];
+    for (int64_t i = 0; i < n; i++) M[i * 2 * n + n + i] = 1.0;
+    for (int64_t c = 0; c < n; c++) {
+        int64_t piv = c;
+        for (int64_t r = c + 1; r < n; r++)
+            if (fabs(M[r * 2 * n + c]) > fabs(M[piv * 2 * n + c])) piv = r;
+        if (piv != c)
+            for (int64_t t = 0; t < 2 * n; t++) {
+                double s = M[c * 2 * n + t];
+                M[c * 2 * n + t] = M[piv * 2 * n + t];
+                M[piv * 2 * n + t] = s;
+            }
+        double d = M[c * 2 * n + c];
+        for (int64_t t = 0; t < 2 * n; t++) M[c * 2 * n + t] /= d;
+        for (int64_t r = 0; r < n; r++) {
+            if (r == c) continue;
+            double f = M[r * 2 * n + c];
+            if (f == 0) continue;
+            for (int64_t t = 0; t < 2 * n; t++) M[r * 2 * n + t] -= f * M[c * 2 * n + t];
+        }
+    }
+    coo_t co = {0};
+    for (int64_t j = 0; j < n; j++)
+        for (int64_t i = 0; i < n; i++) {
+            double v = M[i * 2 * n + n + j];
+            if (!(fabs(v) < atol) && v != 0) coo_push(&co, i, j, v);
+        }
+    free(M);
+    or_mat *R = coo_to_csc(n, n, &co);
+    coo_free(&co);
+    return R;
+}
+
+/* eval_points_1D / nodal2points_1D, src/1d_nodal_basis.jl:183-236: value of
+ * every nodal function at the collocation points (level-major, k per cell:
+ * k-1 nodes taken from the right, then the cell's last point from the left).
+ * The reference evaluates at x +- 1e-16; here at the adjacent double on that
+ * side, which selects the same one-sided limit at every collocation point. */
+static double nodal_side(int k, int level, int cell, int mode, double x, int side) {
+    /* one-sided limit: evaluate at the nearest double on that side */
+    double xs = side > 0 ? nextafter(x, 2.0) : nextafter(x, -1.0);
+    return v_nodal(k, level, cell, mode, xs);
+}
+
+static or_mat *nodal2points_1d(int k, int n, double atol) {
+    int64_t len = (int64_t)k << n;
+    coo_t co = {0};
+    int64_t j = 0;
+    for (int level = 0; level <= n; level++)
+        for (int cell = 1; cell <= (1 << (level > 1 ? level - 1 : 0)); cell++)
+            for (int mode = 1; mode <= k; mode++) {
+                int64_t i = 0;
+                for (int l = 0; l <= n; l++) {
+                    int nc = 1 << (l > 1 ? l - 1 : 0);
+                    for (int c = 1; c <= nc; c++) {
+                        for (int t = 0; t < k - 1; t++) {
+                            double node = l == 0 ? (double)t / (k - 1) : (2.0 * t + 1) / (2.0 * (k - 1));
+                            double x = ((double)(c - 1) + node) / nc;
+                            double val = nodal_side(k, level, cell, mode, x, +1);
+                            if (val != 0) coo_push(&co, i, j, val);
+                            i++;
+                        }
+                        double x = l == 0 ? 1.0 : ((double)c - 0.5) / nc;
+                        double val = nodal_side(k, level, cell, mode, x, -1);
+                        if (val != 0) coo_push(&co, i, j, val);
+                        i++;
+                    }
+                }
+                j++;
+            }
+    or_mat *A = coo_to_csc(len, len, &co);
+    coo_free(&co);
+    or_mat *B = mat_threshold(A, atol);
+    or_mat_free(A);
+    return B;
+}
+
+/* nodal2pos_1D, src/1d_nodal_basis.jl:287-338: inner products of each nodal
+ * function with the finest position basis, integrated on the two halves of
+ * every finest cell that meets the function's cell (Gauss-Legendre, exact for
+ * these polynomial pieces, in place of hquadrature); entries with
+ * |val| <= eps(atol) dropped, then threshold(atol). */
+static or_mat *nodal2pos_1d(int k, int n, double atol) {
+    int64_t len = (int64_t)k << n;
+    const int q = 12;
+    double gx[12], gw[12];
+    gauss_legendre(q, gx, gw);
+    coo_t co = {0};
+    int64_t j = 0;
+    double h = 1.0 / (double)(1LL << n);
+    for (int level = 0; level <= n; level++) {
+        int ncl = 1 << (level > 1 ? level - 1 : 0);
+        for (int cell = 1; cell <= ncl; cell++)
+            for (int mode = 1; mode <= k; mode++) {
+                double nmin = (double)(cell - 1) / ncl, nmax = (double)cell / ncl;
+                for (int c = 1; c <= (1 << n); c++) {
+                    double pmin = (c - 1) * h, pmed = (c - 0.5) * h, pmax = c * h;
+                    if (pmin > nmax || pmax < nmin) continue;
+                    for (int m = 1; m <= k; m++) {
+                        double val = 0.0;
+                        double ab[2][2] = {{pmin, pmed}, {pmed, pmax}};
+                        for (int s = 0; s < 2; s++) {
+                            double a = ab[s][0], b = ab[s][1], acc = 0.0;
+                            for (int t = 0; t < q; t++) {
+                                double x = 0.5 * (a + b) + 0.5 * (b - a) * gx[t];
+                                acc += gw[t] * v_nodal(k, level, cell, mode, x) * or_basis(n, c, m, x);
+                            }
+                            val += acc * 0.5 * (b - a);
+                        }
+                        if (fabs(val) > nextafter(atol, 1.0) - atol) /* eps(atol) */
+                            coo_push(&co, (int64_t)(c - 1) * k + (m - 1), j, val);
+                    }
+                }
+                j++;
+            }
+    }
+    or_mat *A = coo_to_csc(len, len, &co);
+    coo_free(&co);
+    or_mat *B = mat_threshold(A, atol);
+    or_mat_free(A);
+    return B;
+}
+
+/* transform_1D, src/1d_nodal_basis.jl:350-414, for the four maps the Vlasov
+ * evolver uses (atol = 1e-12 as called from transform):
+ *   which 0: modal -> nodal  threshold(pos2nodal_1D(k,n) * hier2pos(k,n), atol)
+ *   which 1: nodal -> points nodal2points_1D(k, n; atol)
+ *   which 2: points -> nodal points2nodal_1D(k, n; atol)
+ *   which 3: nodal -> modal  threshold(pos2hier(k,n) * nodal2pos_1D(k,n), atol) */
+or_mat *or_transform_1d(int k, int n, int which) {
+    or_init();
+    const double atol = 1e-12;
+    if (which == 0) {
+        or_mat *n2pos = nodal2pos_1d(k, n, atol); /* pos2nodal_1D(k, n; atol=1e-12) */
+        or_mat *pos2n = mat_inverse_threshold(n2pos, atol);
+        or_mat *Q = or_hier2pos(k, n);
+        or_mat *P = spmatmul(pos2n, Q);
+        or_mat *R = mat_threshold(P, atol);
+        or_mat_free(n2pos);
+        or_mat_free(pos2n);
+        or_mat_free(Q);
+        or_mat_free(P);
+        return R;
+    }
+    if (which == 1) return nodal2points_1d(k, n, atol);
+    if (which == 2) {
+        or_mat *n2p = nodal2points_1d(k, n, 1e-15);
+        or_mat *R = mat_inverse_threshold(n2p, atol);
+        or_mat_free(n2p);
+        return R;
+    }
+    or_mat *n2pos = nodal2pos_1d(k, n, 1e-15);
+    or_mat *Q = or_hier2pos(k, n);
+    or_mat *Qt = mat_transpose(Q);
+    or_mat *P = spmatmul(Qt, n2pos);
+    or_mat *R = mat_threshold(P, atol);
+    or_mat_free(n2pos);
+    or_mat_free(Q);
+    or_mat_free(Qt);
+    or_mat_free(P);
+    return R;
+}
+
+/* relevant_cell_1D, src/multidim_nodal_basis.jl:19-25 (0-based levels) */
+static int relevant_cell_1d(int level1, int cell1, int level2, int cell2) {
+    double l1 = (double)(cell1 - 1) / (1 << (level1 > 1 ? level1 - 1 : 0));
+    double r1 = (double)cell1 / (1 << (level1 > 1 ? level1 - 1 : 0));
+    double l2 = (double)(cell2 - 1) / (1 << (level2 > 1 ? level2 - 1 : 0));
+    double r2 = (double)cell2 / (1 << (level2 > 1 ? level2 - 1 : 0));
+    return (l1 <= l2 && r1 >= r2) || (l1 >= l2 && r1 <= r2);
+}
+
+/* transform(D, k, n, mat_1D), src/multidim_nodal_basis.jl:40-109: entry
+ * (i, j) = prod_d mat_1D[i_1D(d), j_1D(d)] over pairs of sparse-grid indices
+ * whose cells nest in every dimension; products with |val| < atol = 1e-12
+ * are left out. */
+or_mat *or_transform(int D, int k, int n, int scheme, const or_mat *T1) {
+    idx_t ix;
+    idx_build(&ix, D, k, n, scheme);
+    /* dense 1D matrix (k 2^n square) for direct lookups, as Matrix(mat_1D) */
+    int64_t len = T1->m;
+    double *M1 = calloc((size_t)(len * len), sizeof(double));
+    for (int64_t j = 0; j < T1->n; j++)
+        for (int64_t p = T1->colptr[j]; p < T1->colptr[j + 1]; p++) M1[T1->rowval[p] * len + j] = T1->nzval[p];
+    const double atol = 1e-12;
+    coo_t co = {0};
+    int L1[16], C1[16], Mo1[16], L2[16], C2[16], Mo2[16];
+    int64_t j = 0;
+    for (int t1 = 0; t1 < ix.nlev; t1++) {
+        for (int q = 0; q < D; q++) L1[q] = ix.levels[t1 * D + q];
+        int64_t cells1 = 1;
+        for (int q = 0; q < D; q++) cells1 *= ncells_of(L1[q]);
+        for (int64_t cl1 = 0; cl1 < cells1; cl1++) {
+            int64_t c = cl1;
+            for (int q = 0; q < D; q++) {
+                C1[q] = (int)(c % ncells_of(L1[q])) + 1;
+                c /= ncells_of(L1[q]);
+            }
+            for (int64_t ml1 = 0; ml1 < ix.kD; ml1++) {
+                int64_t mm = ml1;
+                int js[16];
+                for (int q = 0; q < D; q++) {
+                    Mo1[q] = (int)(mm % k) + 1;
+                    mm /= k;
+                    js[q] = k * (int)((L1[q] >= 2 ? (1 << (L1[q] - 2)) : 0) + C1[q] - 1) + Mo1[q] - 1;
+                }
+                int64_t i = 0;
+                for (int t2 = 0; t2 < ix.nlev; t2++) {
+                    for (int q = 0; q < D; q++) L2[q] = ix.levels[t2 * D + q];
+                    int64_t cells2 = 1;
+                    for (int q = 0; q < D; q++) cells2 *= ncells_of(L2[q]);
+                    for (int64_t cl2 = 0; cl2 < cells2; cl2++) {
+                        int64_t cc = cl2;
+                        int rel = 1;
+                        for (int q = 0; q < D; q++) {
+                            C2[q] = (int)(cc % ncells_of(L2[q])) + 1;
+                            cc /= ncells_of(L2[q]);
+                            rel &= relevant_cell_1d(L2[q] - 1, C2[q], L1[q] - 1, C1[q]);
+                        }
+                        if (!rel) {
+                            i += ix.kD;
+                            continue;
+                        }
+                        for (int64_t ml2 = 0; ml2 < ix.kD; ml2++) {
+                            int64_t m2 = ml2;
+                            double val = 1.0;
+                            for (int q = 0; q < D; q++) {
+                                Mo2[q] = (int)(m2 % k) + 1;
+                                m2 /= k;
+                                int i1 = k * (int)((L2[q] >= 2 ? (1 << (L2[q] - 2)) : 0) + C2[q] - 1) + Mo2[q] - 1;
+                                val *= M1[(int64_t)i1 * len + js[q]];
+                                if (val == 0) break;
+                            }
+                            if (!(fabs(val) < atol)) coo_push(&co, i, j, val);
+                            i++;
+                        }
+                    }
+                }
+                j++;
+            }
+        }
+    }
+    free(M1);
+    or_mat *R = coo_to_csc(ix.N, ix.N, &co);
+    coo_free(&co);
+    idx_free(&ix);
+    return R;
+}

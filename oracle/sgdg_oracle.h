@@ -49,4 +49,9 @@ void or_tensor_construct(int D, int k, int n, int scheme, const double *coeffs1d
 int or_cell_index(double x, int l);
 void or_reconstruct(int D, int k, int n, int scheme, const double *coeffs, int64_t npts, const double *pts,
                     double *out);
+
+/* nodal basis transforms (src/1d_nodal_basis.jl, src/multidim_nodal_basis.jl):
+ * which 0 modal->nodal, 1 nodal->points, 2 points->nodal, 3 nodal->modal */
+or_mat *or_transform_1d(int k, int n, int which);
+or_mat *or_transform(int D, int k, int n, int scheme, const or_mat *T1);
 #endif
