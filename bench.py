@@ -238,8 +238,8 @@ def vlasov_leg(sg, steps):
     _, st = sg.vlasov_evolve(Dx, k, n, F, f0, 0.0, steps * dt, nsteps=steps, op=op)
     total = time.perf_counter() - t1
     per_step = max(total - one, 1e-9) / max(steps - 1, 1)
-    nnz = {w: int(op.transform(*w).nnz) for w in [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"),
-                                                   ("nodal", "modal")]}
+    nnz = {"%s_to_%s" % w: int(op.transform(*w).nnz)
+           for w in [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"), ("nodal", "modal")]}
     op.close()
     return {"workload": "Vlasov 2x2v (D=4 phase space), sparse k=2, n=8, RK4", "state_dofs": int(f0.size),
             "steps": steps, "dt": dt, "form": "FP64 sparse operators (CSR SpMV), graph per RK4 step",

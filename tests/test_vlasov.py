@@ -95,7 +95,7 @@ def test_vlasov_rhs_matches_oracle(sgdg, O, W, D, k, n):
     op = sgdg.VlasovOperator(D, k, n)
     got = op.rhs(F, f0)
     ref = O.vlasov_rhs(D, k, n, oracle_ops(O, D, k, n), F, f0)
-    assert rel(got, ref) < 1e-12
+    assert rel(got, ref) < 1e-10  # FP64, chained SpMVs with cancellation; GPU uses FMA
 
 
 @pytest.mark.gpu
