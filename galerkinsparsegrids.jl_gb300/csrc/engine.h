@@ -22,11 +22,12 @@ struct DevCSR {
 // solves' vectors in arenas (slot-major: slot s owns [s*Ns, (s+1)*Ns)), so a
 // tile may take columns from several solves.  One launch per RK stage runs an
 // ordered work list: for every group of slots, one pass per dimension (pencil
-// tiles: sweep the 1D operator, accumulate into rhs) and then the RK update
-// of the group; each phase waits for the previous phase of its group.
+// tiles: sweep the 1D operator, accumulate into rhs); the last pass applies the
+// RK stage update to the elements it completes.  Each phase waits for the
+// previous phase of its group.
 enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1 };
-enum : int { TILE_FIRST = 1, TILE_LAST = 2 };
-enum : int { ITEM_PASS = 0, ITEM_RK = 1 };
+enum : int { TILE_FIRST = 1, TILE_LAST = 2, TILE_RK = 4 };  // TILE_RK: last pass with the RK4 update fused
+enum : int { ITEM_PASS = 0 };
 
 struct MFClass {
     const int32_t* s_rowptr;  // 1D operator, block CSR over 2^n row blocks (2^n + 1 entries)
@@ -55,19 +56,19 @@ inline int mf_table_bytes(int nrow, int nent, int nval) {
 constexpr int kMFTableSmemMax = 48 * 1024;
 
 struct MFItem {
-    int16_t type;      // ITEM_PASS / ITEM_RK
+    int16_t type;      // ITEM_PASS
     int16_t cls;
     int16_t d;         // pass: 0-based dimension
-    int16_t flags;     // pass: TILE_FIRST | TILE_LAST
+    int16_t flags;     // pass: TILE_FIRST | TILE_LAST | TILE_RK
     int32_t wait_ctr;  // counter to wait for (-1: none) ...
     int32_t wait_need; // ... until it reaches this value
     int32_t done_ctr;  // counter incremented when the item is done
     int32_t lmax;      // pass: 1-based max level of the pencil along d
     int32_t lp;        // pass: log2 prod_{q<d} cells_q
     int32_t boff;      // pass: first level-block offset of the pencil in blockoff
-    int32_t R;         // pass: columns per solve;  RK: slot
-    int32_t g0;        // pass: first class column (slot*R + r);  RK: first element
-    int32_t W;         // pass: columns (multiple of the per-thread column count);  RK: end element
+    int32_t R;         // pass: columns per solve
+    int32_t g0;        // pass: first class column (slot*R + r)
+    int32_t W;         // pass: columns (multiple of the per-thread column count)
     int32_t Wv;        // pass: valid columns
     int32_t kd1;       // pass: k^d
     int32_t kDm1;      // pass: k^(D-1)

@@ -1,24 +1,26 @@
 // mf.cu -- the matrix-free form: one persistent launch per RK4 stage.
 //
 // The launch walks an ordered work list (engine.h): for each group of solves
-// of a class, one pass per dimension d and then the group's RK update.  A
-// pass item is a pencil tile: the pencil's 1D prefix (m = k 2^(lmax-1) rows)
-// times W columns taken across the group's solves.  The tile is gathered into
-// shared memory with cp.async, swept with the 1D operator's k x k blocks
-// (stored as FP32 hi + lo pairs and applied with the paired FMA __ffma2_rn,
-// so the operator carries ~FP64 entries while the data stays FP32), and the
-// result is added into the FP32 partial-sum vector rhs (L2-resident for the
-// group, accessed with .cg so other SMs' writes are seen).  For the wave
-// (u_tt = sum_d D_d D_d u) the tile applies the 1D operator twice.  The RK
-// item streams the group's FP64 state once: k from rhs (and, for the wave's
-// displacement field, from the stage input of the velocity field), then the
-// stage combination and the FP32 stage input of the next stage.
+// of a class, one pass per dimension d.  A pass item is a pencil tile: the
+// pencil's 1D prefix (m = k 2^(lmax-1) rows) times W columns taken across the
+// group's solves.  The tile is gathered into shared memory with cp.async,
+// swept with the 1D operator's k x k blocks (stored as FP32 hi + lo pairs and
+// applied with the paired FMA __ffma2_rn, so the operator carries ~FP64
+// entries while the data stays FP32), and the result is added into the FP32
+// partial-sum vector rhs (L2-resident for the group, accessed with .cg so
+// other SMs' writes are seen).  For the wave (u_tt = sum_d D_d D_d u) the
+// tile applies the 1D operator twice.  The last dimension's tile completes
+// the right-hand side of its elements and applies the RK stage update to
+// them in place: FP64 state, the stage combination, and the FP32 stage input
+// of the next stage (for the wave also the displacement field, whose
+// derivative is the velocity's stage input).
 //
-// Ordering: items are handed out in list order by an atomic counter; an item
-// of phase p waits (bounded spin) until every item of phase p-1 of its group
-// has finished, so progress never depends on a later item.  A wait that runs
-// out sets *err and skips the item.
+// Ordering: items are handed out in list order by an atomic counter; an item of phase p waits (bounded spin) until every item of
+// phase p-1 of its group has finished, so progress never depends on a later
+// item.  A wait that runs out sets *err and skips the item.
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include "engine.h"
 #include "rk.cuh"
@@ -175,9 +177,10 @@ __device__ __forceinline__ void wait_counter(const int* ctr, int need, int* err)
     }
 }
 
+// One pencil tile; sboff holds the pencil's level-block offsets.
 template <int K, int CPT, bool WAVE>
-__device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int in_sel, float* smem, const int* ctr,
-                          int* err) {
+__device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, const int* sboff, int stage,
+                          int in_sel, float* smem, const int* ctr, int* err) {
     const int tid = threadIdx.x;
     const int nrb = 1 << (it.lmax - 1);
     const int m = nrb * K;
@@ -189,15 +192,15 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     float* X = reinterpret_cast<float*>(cb + W);  // 12W bytes in: 16-aligned for W % 4 == 0, 8 for W % 2 == 0
     float* Y = X + m * W;
     const int kD = C.kD, kd1 = it.kd1, lp = it.lp, R = it.R, kDm1 = it.kDm1;
-    __shared__ int sboff[32];
-    if (tid < it.lmax) sboff[tid] = (int)C.blockoff[it.boff + tid];  // level-block offsets (N < 2^31)
     for (int j = tid; j < W; j += kMFThreads) {
         if (j < Wv) {
+            // column g of the class: slot, then (cells, modes) of the other dimensions
             const int g = it.g0 + j;
             const int slot = g / R, r = g - slot * R;
-            const int mr = r % kDm1, cr = r / kDm1;
+            const int cr = r / kDm1, mr = r - cr * kDm1;
+            const int mq = mr / kd1;
             cslot[j] = slot;
-            ca[j] = kD * (cr & ((1 << lp) - 1)) + (mr % kd1) + (mr / kd1) * kd1 * K;
+            ca[j] = kD * (cr & ((1 << lp) - 1)) + (mr - mq * kd1) + mq * kd1 * K;
             cb[j] = kD * ((cr >> lp) << lp);
         } else {
             cslot[j] = -1;
@@ -247,55 +250,62 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     if (it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
     const bool first = (it.flags & TILE_FIRST) != 0;
+    if (!(it.flags & TILE_RK)) {
+        // partial sum sum_{q <= d} coef_q D_q u of this tile's elements
+        for (int e = tid; e < ne; e += kMFThreads) {
+            const int row = e >> lw, j = e & (W - 1);
+            const int s = cslot[j];
+            if (s < 0) continue;
+            const int rb = row / K, i = row - rb * K;
+            float* rp = C.rhs + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
+            const float z = Z[e];
+            float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
+            if (!first) v += __ldcg(rp);
+            __stcg(rp, v);
+        }
+        return;
+    }
+    // last dimension: the right-hand side of each element is complete here, so
+    // the RK4 stage update of its state runs in place (for the wave also the
+    // element's f component, whose derivative is the stage input of v).  The
+    // pencils of one dimension partition the coefficients, so every state
+    // element is updated once per stage.
+    float* __restrict__ uout = C.u[in_sel ^ 1];
     for (int e = tid; e < ne; e += kMFThreads) {
         const int row = e >> lw, j = e & (W - 1);
         const int s = cslot[j];
-        if (s < 0) continue;
+        if (s < 0 || __ldg(C.status + s) != 0) continue;
         const int rb = row / K, i = row - rb * K;
-        float* rp = C.rhs + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
+        const int off = elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
+        const size_t b = (size_t)s * C.Ns;
+        const size_t iv = b + (WAVE ? (size_t)C.N : 0) + off;  // the component D acts on
+        // issue every load of the element before the arithmetic
         const float z = Z[e];
-        float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
-        if (!first) v += __ldcg(rp);
-        __stcg(rp, v);
-    }
-}
-
-__device__ void rk_chunk(const MFItem& it, const MFClass& C, int stage, int in_sel) {
-    const int slot = it.R;
-    if (C.status[slot] != 0) return;
-    const double dt = C.dt[slot];
-    const size_t base = (size_t)slot * C.Ns;
-    double* __restrict__ y = C.y + base;
-    double* __restrict__ acc = C.acc + base;
-    const float* __restrict__ uin = C.u[in_sel] + base;
-    float* __restrict__ uout = C.u[in_sel ^ 1] + base;
-    const float* rhs = C.rhs + (size_t)slot * C.N;
-    const int N = C.N;
-    const bool wave = C.kind == MF_KIND_WAVE;
-    for (int e0 = it.g0 + (int)threadIdx.x; e0 < it.W; e0 += 4 * kMFThreads) {
-        double kk[4], yy[4], aa[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int e = e0 + u * kMFThreads;
-            kk[u] = yy[u] = aa[u] = 0.0;
-            if (e < it.W) {
-                kk[u] = wave ? (e < N ? (double)uin[N + e] : (double)__ldcg(rhs + (e - N))) : (double)__ldcg(rhs + e);
-                yy[u] = y[e];
-                if (stage != 1) aa[u] = acc[e];
-            }
+        const float prev = first ? 0.f : __ldcg(C.rhs + (size_t)s * C.N + off);
+        double yv = __ldcg(C.y + iv), av = stage != 1 ? __ldcg(C.acc + iv) : 0.0;
+        double yf = 0.0, af = 0.0, kf = 0.0;
+        if (WAVE) {
+            yf = __ldcg(C.y + b + off);
+            af = stage != 1 ? __ldcg(C.acc + b + off) : 0.0;
+            kf = (double)__ldcg(uin + b + C.N + off);
         }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int e = e0 + u * kMFThreads;
-            if (e < it.W) {
-                double un;
-                rk_stage(stage, dt, kk[u], yy[u], aa[u], un);
-                if (stage == 4)
-                    y[e] = yy[u];
-                else
-                    acc[e] = aa[u];
-                uout[e] = (float)un;
-            }
+        float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
+        if (!first) v += prev;
+        const double dt = __ldg(C.dt + s);
+        double un;
+        rk_stage(stage, dt, (double)v, yv, av, un);
+        if (stage == 4)
+            __stcg(C.y + iv, yv);
+        else
+            __stcg(C.acc + iv, av);
+        __stcg(uout + iv, (float)un);
+        if (WAVE) {
+            rk_stage(stage, dt, kf, yf, af, un);
+            if (stage == 4)
+                __stcg(C.y + b + off, yf);
+            else
+                __stcg(C.acc + b + off, af);
+            __stcg(uout + b + off, (float)un);
         }
     }
 }
@@ -307,25 +317,33 @@ __global__ void __launch_bounds__(kMFThreads, 6)
     extern __shared__ __align__(16) float smem[];
     float* tile = smem + table_bytes / 4;
     __shared__ int s_item;
-    __shared__ int s_cached;  // class whose table is in shared memory (-1: none)
     __shared__ MFItem s_it;
     __shared__ MFClass s_cls;
+    __shared__ int s_cls_id;   // class in s_cls (-1: none)
+    __shared__ int s_cached;   // class whose table is in shared memory (-1: none)
+    __shared__ int s_off[32];  // level-block offsets of the item's pencil (N < 2^31)
     const int tid = threadIdx.x;
     constexpr int kItemWords = sizeof(MFItem) / 4;
     constexpr int kClsWords = sizeof(MFClass) / 4;
     static_assert(kItemWords <= 32, "item fits one warp");
-    if (tid == 0) s_cached = -1;
+    if (tid == 0) s_cls_id = s_cached = -1;
     for (;;) {
-        // warp 0 takes the next item and stages it and its class descriptor
+        // warp 0 takes the next item and stages it (and its class descriptor
+        // when the class changes)
         if (tid < 32) {
             int ii = 0;
             if (tid == 0) ii = atomicAdd(ctr, 1);
             ii = __shfl_sync(0xffffffffu, ii, 0);
             if (ii < nitems) {
-                if (tid < kItemWords) reinterpret_cast<int*>(&s_it)[tid] = reinterpret_cast<const int*>(items + ii)[tid];
-                const int cls = items[ii].cls;
-                for (int w = tid; w < kClsWords; w += 32)
-                    reinterpret_cast<int*>(&s_cls)[w] = reinterpret_cast<const int*>(classes + cls)[w];
+                int word = 0;
+                if (tid < kItemWords) {
+                    word = reinterpret_cast<const int*>(items + ii)[tid];
+                    reinterpret_cast<int*>(&s_it)[tid] = word;
+                }
+                const int cls = __shfl_sync(0xffffffffu, word, 0) >> 16;  // MFItem::cls (second int16)
+                if (cls != s_cls_id)
+                    for (int w = tid; w < kClsWords; w += 32)
+                        reinterpret_cast<int*>(&s_cls)[w] = reinterpret_cast<const int*>(classes + cls)[w];
             }
             if (tid == 0) s_item = ii;
         }
@@ -333,39 +351,35 @@ __global__ void __launch_bounds__(kMFThreads, 6)
         if (s_item >= nitems) break;
         const MFItem& it = s_it;
         const MFClass& C = s_cls;
-        if (it.type == ITEM_RK) {
-            if (it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
-            __syncthreads();
-            rk_chunk(it, C, stage, in_sel);
-        } else {
-            OpTable T{C.s_rowptr, C.s_ent, C.s_val};
-            if (C.s_shared) {
-                int* trow = reinterpret_cast<int*>(smem);
-                int* tent = trow + C.s_nrow;
-                float* tval = smem + (((C.s_nrow + C.s_nent) * 4 + 15) / 16) * 4;
-                if (s_cached != it.cls) {  // copy the class's operator table (uniform branch)
-                    for (int i = tid; i < C.s_nrow; i += kMFThreads) trow[i] = C.s_rowptr[i];
-                    for (int i = tid; i < C.s_nent; i += kMFThreads) tent[i] = C.s_ent[i];
-                    for (int i = tid; i < C.s_nval / 4; i += kMFThreads)
-                        reinterpret_cast<float4*>(tval)[i] = reinterpret_cast<const float4*>(C.s_val)[i];
-                    __syncthreads();
-                    if (tid == 0) s_cached = it.cls;
-                }
-                T = OpTable{trow, tent, tval};
+        if (tid == 0) s_cls_id = it.cls;  // read again only after the next barrier
+        if (tid < it.lmax) s_off[tid] = (int)C.blockoff[it.boff + tid];  // seen after pass_tile's first barrier
+        OpTable T{C.s_rowptr, C.s_ent, C.s_val};
+        if (C.s_shared) {
+            int* trow = reinterpret_cast<int*>(smem);
+            int* tent = trow + C.s_nrow;
+            float* tval = smem + (((C.s_nrow + C.s_nent) * 4 + 15) / 16) * 4;
+            if (s_cached != it.cls) {  // copy the class's operator table (uniform branch)
+                for (int i = tid; i < C.s_nrow; i += kMFThreads) trow[i] = C.s_rowptr[i];
+                for (int i = tid; i < C.s_nent; i += kMFThreads) tent[i] = C.s_ent[i];
+                for (int i = tid; i < C.s_nval / 4; i += kMFThreads)
+                    reinterpret_cast<float4*>(tval)[i] = reinterpret_cast<const float4*>(C.s_val)[i];
+                __syncthreads();
+                if (tid == 0) s_cached = it.cls;
             }
-            switch (C.k * 2 + C.kind) {
-                case 2: pass_tile<1, 4, false>(it, C, T, in_sel, tile, ctr, err); break;
-                case 3: pass_tile<1, 4, true>(it, C, T, in_sel, tile, ctr, err); break;
-                case 4: pass_tile<2, 4, false>(it, C, T, in_sel, tile, ctr, err); break;
-                case 5: pass_tile<2, 4, true>(it, C, T, in_sel, tile, ctr, err); break;
-                case 6: pass_tile<3, 4, false>(it, C, T, in_sel, tile, ctr, err); break;
-                case 7: pass_tile<3, 4, true>(it, C, T, in_sel, tile, ctr, err); break;
-                case 8: pass_tile<4, 2, false>(it, C, T, in_sel, tile, ctr, err); break;
-                case 9: pass_tile<4, 2, true>(it, C, T, in_sel, tile, ctr, err); break;
-                case 10: pass_tile<5, 2, false>(it, C, T, in_sel, tile, ctr, err); break;
-                case 11: pass_tile<5, 2, true>(it, C, T, in_sel, tile, ctr, err); break;
-                default: break;
-            }
+            T = OpTable{trow, tent, tval};
+        }
+        switch (C.k * 2 + C.kind) {
+            case 2: pass_tile<1, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 3: pass_tile<1, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 4: pass_tile<2, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 5: pass_tile<2, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 6: pass_tile<3, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 7: pass_tile<3, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 8: pass_tile<4, 2, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 9: pass_tile<4, 2, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 10: pass_tile<5, 2, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 11: pass_tile<5, 2, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            default: break;
         }
         __syncthreads();
         if (tid == 0) {

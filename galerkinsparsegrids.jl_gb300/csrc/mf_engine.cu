@@ -24,7 +24,6 @@ cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
 
 static constexpr int64_t kGroupReuseBytes = 6LL << 20;  // reused u + rhs per group (~4 groups in flight)
-static constexpr int kRKChunk = 8192;
 
 // The arenas' cudaFree calls wait for outstanding work; the stream is not
 // touched here because a caller's stream may already be gone.
@@ -315,8 +314,9 @@ void MFEngine::plan() {
 }
 
 // Work list.  Each class is cut into groups of slots; a group has one phase
-// per dimension pass and (unless applying only) an RK phase, and phase p of a
-// group depends on phase p-1 of the same group.  Groups are emitted in
+// per dimension pass (the last one also applies the RK stage update, unless
+// applying only), and phase p of a group depends on phase p-1 of the same
+// group.  Groups are emitted in
 // wavefront order -- step t holds phase t-g of group g, oldest group first --
 // so when a phase is handed out, its predecessor was handed out a whole
 // wavefront earlier and is normally complete: CTAs rarely wait, while the
@@ -370,7 +370,10 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                         it.type = ITEM_PASS;
                         it.cls = (int16_t)ci;
                         it.d = (int16_t)d;
-                        it.flags = (int16_t)((ph == 0 ? TILE_FIRST : 0) | (ph + 1 == dims.size() ? TILE_LAST : 0));
+                        const bool last = ph + 1 == dims.size();
+                        // the last pass updates the RK state (never while tuning: no state changes)
+                        it.flags = (int16_t)((ph == 0 ? TILE_FIRST : 0) | (last ? TILE_LAST : 0) |
+                                             (last && !sp.apply && !pass_only ? TILE_RK : 0));
                         it.lmax = p.lmax;
                         it.lp = p.lp;
                         it.boff = c.boff_index[bi + pi];
@@ -384,20 +387,6 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                         list.push_back(it);
                     }
                 }
-                grp.phases.push_back(std::move(list));
-            }
-            if (!sp.apply && !pass_only) {
-                std::vector<MFItem> list;
-                for (int sl = s0; sl < s1; sl++)
-                    for (int64_t e0 = 0; e0 < c.Ns; e0 += kRKChunk) {
-                        MFItem it{};
-                        it.type = ITEM_RK;
-                        it.cls = (int16_t)ci;
-                        it.R = sl;
-                        it.g0 = (int32_t)e0;
-                        it.W = (int32_t)std::min<int64_t>(c.Ns, e0 + kRKChunk);
-                        list.push_back(it);
-                    }
                 grp.phases.push_back(std::move(list));
             }
             groups.push_back(std::move(grp));
