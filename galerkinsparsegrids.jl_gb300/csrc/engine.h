@@ -38,7 +38,7 @@ struct MFClass {
     double* acc;
     float* u[2];
     float* rhs;               // nslots * N
-    const double* dt;         // per slot
+    const double* dt;         // per slot: dt, dt / 2, dt / 6
     const float* coef;        // per slot, 16 entries: factor on D_d as hi[8], lo[8]
     const int32_t* status;    // per slot, nonzero = skip the RK update
     int32_t N, Ns;

@@ -34,14 +34,15 @@ __global__ void __launch_bounds__(256) k_csr_spmv(DevCSR A, const double* __rest
 
 template <int VS>
 __global__ void __launch_bounds__(256) k_csr_rk4(DevCSR A, const double* uin, double* y, double* __restrict__ acc,
-                                                 double* __restrict__ uout, double dt, int stage) {
+                                                 double* __restrict__ uout, double dt, double hdt, double dt6,
+                                                 int stage) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = t / VS;
     const int lane = int(t % VS);
     double k = csr_row<VS>(A, row, uin, lane);
     if (row < A.m && lane == 0) {
         double yy = y[row], aa = stage == 1 ? 0.0 : acc[row], un;
-        rk_stage(stage, dt, k, yy, aa, un);
+        rk_stage(stage, dt, hdt, dt6, k, yy, aa, un);
         if (stage == 4)
             y[row] = yy;
         else {
@@ -94,13 +95,14 @@ cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStr
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
                            int stage, cudaStream_t st) {
     const int64_t th = A.m * A.vs;
+    const double hdt = 0.5 * dt, dt6 = dt / 6.0;
     switch (A.vs) {
-        case 1: k_csr_rk4<1><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, stage); break;
-        case 2: k_csr_rk4<2><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, stage); break;
-        case 4: k_csr_rk4<4><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, stage); break;
-        case 8: k_csr_rk4<8><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, stage); break;
-        case 16: k_csr_rk4<16><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, stage); break;
-        default: k_csr_rk4<32><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, stage); break;
+        case 1: k_csr_rk4<1><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
+        case 2: k_csr_rk4<2><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
+        case 4: k_csr_rk4<4><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
+        case 8: k_csr_rk4<8><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
+        case 16: k_csr_rk4<16><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
+        default: k_csr_rk4<32><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
     }
     return cudaGetLastError();
 }

@@ -291,16 +291,16 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         }
         float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
         if (!first) v += prev;
-        const double dt = __ldg(C.dt + s);
+        const double dt = __ldg(C.dt + 3 * s), hdt = __ldg(C.dt + 3 * s + 1), dt6 = __ldg(C.dt + 3 * s + 2);
         double un;
-        rk_stage(stage, dt, (double)v, yv, av, un);
+        rk_stage(stage, dt, hdt, dt6, (double)v, yv, av, un);
         if (stage == 4)
             __stcg(C.y + iv, yv);
         else
             __stcg(C.acc + iv, av);
         __stcg(uout + iv, (float)un);
         if (WAVE) {
-            rk_stage(stage, dt, kf, yf, af, un);
+            rk_stage(stage, dt, hdt, dt6, kf, yf, af, un);
             if (stage == 4)
                 __stcg(C.y + b + off, yf);
             else

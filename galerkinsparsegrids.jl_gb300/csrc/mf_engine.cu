@@ -213,12 +213,14 @@ void MFEngine::plan() {
         c.u0.alloc(sizeof(float) * ns * c.Ns);
         c.u1.alloc(sizeof(float) * ns * c.Ns);
         c.rhs.alloc(sizeof(float) * ns * c.N);
-        std::vector<double> dt(ns);
+        std::vector<double> dt(3 * (size_t)ns);
         std::vector<float> coef((size_t)ns * 16, 0.f);
         std::vector<int32_t> status(ns, 0);
         for (int sl = 0; sl < ns; sl++) {
             Solve& s = solves_[c.slots[sl]];
-            dt[sl] = s.spec.dt;
+            dt[3 * sl] = s.spec.dt;
+            dt[3 * sl + 1] = 0.5 * s.spec.dt;
+            dt[3 * sl + 2] = s.spec.dt / 6.0;
             for (int d = 0; d < 8; d++) {
                 // factor on D_d as an FP32 (hi, lo) pair: a rounded velocity
                 // would perturb the operator systematically

@@ -189,7 +189,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         const Region r_boff = L.add(sizeof(int64_t) * boff.size());
         const Region r_coef = L.add(sizeof(float) * 16);
         const Region r_status = L.add(sizeof(int32_t));
-        const Region r_dt = L.add(sizeof(double));
+        const Region r_dt = L.add(sizeof(double) * 3);
         const Region r_u = L.add(sizeof(float) * (size_t)N);
         const Region r_rhs = L.add(sizeof(float) * (size_t)N);
         if (L.top > kNoAllocScratchBytes)
@@ -228,7 +228,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         c.rs = rs;
         const float coef[16] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int32_t status = 0;
-        const double dt = 0.0;
+        const double dt[3] = {0.0, 0.0, 0.0};
 
         // every region this call reads is rewritten; counters and the error
         // flag start at zero (launch_mf_stage clears the counters)
@@ -244,7 +244,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                                {r_boff, boff.data()},
                                {r_coef, coef},
                                {r_status, &status},
-                               {r_dt, &dt}};
+                               {r_dt, dt}};
         for (const Copy& cp : copies)
             if (cp.r.bytes) {
                 e = cudaMemcpyAsync(base + cp.r.off, cp.src, cp.r.bytes, cudaMemcpyHostToDevice, st);
