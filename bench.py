@@ -212,7 +212,7 @@ def uneven_batch_leg(sg, stream, steps=50, warmup=5):
             "working_set_bytes": int(28 * total), "steps": steps,
             "default_tiles": {"value": dofs / (ms_default / 1e3), "ms_per_step": ms_default},
             "autotuned_tiles": {"value": dofs / (ms_tuned / 1e3), "ms_per_step": ms_tuned},
-            "shapes_wmult_coop": shapes}
+            "shapes_wlog_coop": shapes}
 
 
 def vlasov_leg(sg, steps):
@@ -484,7 +484,7 @@ def run_ours(args):
                        "ms_per_step": 1e3 * plain_s / args.steps},
         "clocks": clocks,
     }
-    line["config"]["tile_shape_wmult_coop"] = list(tile[:2])
+    line["config"]["tile_shape_wlog_coop"] = list(tile[:2])
     line["uneven_batch"] = uneven_batch_leg(sg, stream)
     if args.vlasov_steps > 0:
         line["vlasov"] = vlasov_leg(sg, args.vlasov_steps)

@@ -667,14 +667,15 @@ class Server:
 
 
 def tile_shape(D, k):
-    """(wmult, coop, tuned) of the pencil tiles of (D, k)."""
+    """(wlog, coop, tuned) of the pencil tiles of (D, k): 2^wlog scales the
+    tile width, row levels <= lmax - coop are swept by whole warps."""
     w, c, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     check(lib().sgdg_tile_shape(D, k, ctypes.byref(w), ctypes.byref(c), ctypes.byref(t)))
     return w.value, c.value, bool(t.value)
 
 
-def set_tile_shape(D, k, wmult, coop):
-    check(lib().sgdg_set_tile_shape(D, k, wmult, coop))
+def set_tile_shape(D, k, wlog, coop):
+    check(lib().sgdg_set_tile_shape(D, k, wlog, coop))
 
 
 def clear_tile_shapes():

@@ -750,19 +750,19 @@ int sgdg_batch_autotune(sgdg_batch* b, int* ntuned) {
     API_END
 }
 
-int sgdg_tile_shape(int D, int k, int* wmult, int* coop, int* tuned) {
+int sgdg_tile_shape(int D, int k, int* wlog, int* coop, int* tuned) {
     API_BEGIN
     const MFTile t = mf_tile(D, k);
-    if (wmult) *wmult = t.wmult;
+    if (wlog) *wlog = t.wlog;
     if (coop) *coop = t.coop;
     if (tuned) *tuned = mf_tile_tuned(D, k) ? 1 : 0;
     API_END
 }
 
-int sgdg_set_tile_shape(int D, int k, int wmult, int coop) {
+int sgdg_set_tile_shape(int D, int k, int wlog, int coop) {
     API_BEGIN
     if (D < 1 || D > 8 || k < 1 || k > 5) throw Error(SGDG_EINVAL, "tile shapes exist for 1 <= D <= 8, 1 <= k <= 5");
-    mf_set_tile(D, k, MFTile{wmult, coop});
+    mf_set_tile(D, k, MFTile{wlog, coop});
     API_END
 }
 

@@ -79,12 +79,15 @@ constexpr int kMFThreads = 128;
 constexpr int kSpinLimit = 1 << 22;  // polls of a dependency counter before giving up
 
 // Tile shape of the pass tiles of one (D, k), chosen by the autotuner:
-// a tile has cpt * max(1, 128 / nrb) * wmult columns (nrb = row blocks of the
-// pencil), and the row blocks of levels <= lmax - coop are warp-cooperative.
+// a tile has cpt * max(1, 128 / nrb) * 2^wlog columns (at least cpt; nrb =
+// row blocks of the pencil), and the row blocks of levels <= lmax - coop are
+// warp-cooperative.  Narrower tiles need less shared memory (more CTAs per
+// SM), wider ones amortise each item's fixed cost.
 struct MFTile {
-    int wmult = 1;
+    int wlog = 0;
     int coop = 4;
 };
+constexpr int kMFWlogMin = -2, kMFWlogMax = 3;
 MFTile mf_tile(int D, int k);                 // tuned shape, or the default
 bool mf_tile_tuned(int D, int k);
 void mf_set_tile(int D, int k, const MFTile& t);
@@ -95,8 +98,10 @@ inline int mf_rlong(int lmax, int coop) { return lmax > coop ? 1 << (lmax - 1 - 
 inline size_t mf_tile_smem(int k, int nrb, int W) { return 4 * (3 * (size_t)W + (size_t)k * nrb * W * 2); }
 constexpr size_t kMFTileSmemMax = 64 * 1024;  // wider tiles are narrowed to fit
 // columns of a pass tile (a power of two)
-inline int mf_tile_cols(int k, int cpt, int nrb, int wmult) {
-    int W = cpt * (nrb < kMFThreads ? kMFThreads / nrb : 1) * wmult;
+inline int mf_tile_cols(int k, int cpt, int nrb, int wlog) {
+    int W = cpt * (nrb < kMFThreads ? kMFThreads / nrb : 1);
+    W = wlog >= 0 ? W << wlog : W >> -wlog;
+    if (W < cpt) W = cpt;
     while (W > cpt && mf_tile_smem(k, nrb, W) > kMFTileSmemMax) W >>= 1;
     return W;
 }

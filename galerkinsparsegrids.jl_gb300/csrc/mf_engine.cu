@@ -364,7 +364,7 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                 for (size_t pi = 0; pi < c.pencils[d].size(); pi++) {
                     const Pencil& p = c.pencils[d][pi];
                     const int nrb = 1 << (p.lmax - 1);
-                    const int Wp = mf_tile_cols(k, cpt, nrb, tile.wmult);
+                    const int Wp = mf_tile_cols(k, cpt, nrb, tile.wlog);
                     const int64_t cbeg = (int64_t)s0 * p.R, cend = (int64_t)s1 * p.R;
                     smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
                     for (int64_t g0 = cbeg; g0 < cend; g0 += Wp) {
@@ -441,8 +441,8 @@ bool mf_tile_tuned(int D, int k) {
 }
 
 void mf_set_tile(int D, int k, const MFTile& t) {
-    if (t.wmult < 1 || t.wmult > 64 || (t.wmult & (t.wmult - 1)) || t.coop < 1 || t.coop > 30)
-        throw Error(SGDG_EINVAL, "tile shape: wmult must be a power of two in 1..64 and coop in 1..30");
+    if (t.wlog < kMFWlogMin || t.wlog > kMFWlogMax || t.coop < 1 || t.coop > 30)
+        throw Error(SGDG_EINVAL, "tile shape: wlog must be in -2..3 and coop in 1..30");
     std::lock_guard<std::mutex> g(g_tile_mu);
     g_tiles[{D, k}] = t;
 }
@@ -502,10 +502,10 @@ std::vector<std::pair<int, int>> MFEngine::autotune() {
             MFTile best = mf_tile(dk.first, dk.second);
             shapes[dk] = best;
             float tbest = time_shapes();
-            for (int wmult : {1, 2, 4, 8})
+            for (int wlog = kMFWlogMin; wlog <= kMFWlogMax; wlog++)
                 for (int coop : {3, 4, 5, 6}) {
-                    const MFTile cand{wmult, coop};
-                    if (cand.wmult == best.wmult && cand.coop == best.coop) continue;
+                    const MFTile cand{wlog, coop};
+                    if (cand.wlog == best.wlog && cand.coop == best.coop) continue;
                     shapes[dk] = cand;
                     const float t = time_shapes();
                     if (t < 0.98f * tbest) {

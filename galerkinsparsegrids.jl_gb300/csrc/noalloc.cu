@@ -140,7 +140,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                 const int32_t pb = (int32_t)boff.size();
                 for (auto o : p.blockoff) boff.push_back(o);
                 const int nrb = 1 << (p.lmax - 1);
-                const int Wp = mf_tile_cols(k, cpt, nrb, tile.wmult);
+                const int Wp = mf_tile_cols(k, cpt, nrb, tile.wlog);
                 smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
                 for (int64_t g0 = 0; g0 < p.R; g0 += Wp) {
                     MFItem it{};

@@ -183,17 +183,18 @@ int sgdg_batch_upload(sgdg_batch *b, const double *y_all);
 int sgdg_batch_download(sgdg_batch *b, double *y_all);
 /* Autotuner: for every (D, k) of the batch's solves that has no tuned tile
  * shape yet, times one RK stage's pencil tiles of the whole batch for each
- * candidate shape (tile width multiplier 1, 2, 4, 8 x warp-cooperative row
- * levels 3..6; no state changes) and keeps the fastest in a process-wide
+ * candidate shape (tile width factor 2^wlog, wlog -2..3, x warp-cooperative
+ * row levels 3..6; no state changes) and keeps the fastest in a process-wide
  * table that every batch, server and sgdg_apply_noalloc call then uses.
  * *ntuned = number of (D, k) tuned by this call. */
 int sgdg_batch_autotune(sgdg_batch *b, int *ntuned);
 /* The tile shape used for (D, k): columns per tile = c * max(1, 128 / row
- * blocks) * wmult, row blocks of levels <= lmax - coop swept by whole warps;
- * *tuned = 1 if it came from the autotuner or sgdg_set_tile_shape. */
-int sgdg_tile_shape(int D, int k, int *wmult, int *coop, int *tuned);
-/* Pins a tile shape for (D, k) (wmult a power of two in 1..64, coop 1..30). */
-int sgdg_set_tile_shape(int D, int k, int wmult, int coop);
+ * blocks) * 2^wlog (at least c), row blocks of levels <= lmax - coop swept by
+ * whole warps; *tuned = 1 if it came from the autotuner or
+ * sgdg_set_tile_shape. */
+int sgdg_tile_shape(int D, int k, int *wlog, int *coop, int *tuned);
+/* Pins a tile shape for (D, k) (wlog -2..3, coop 1..30). */
+int sgdg_set_tile_shape(int D, int k, int wlog, int coop);
 /* Forgets every tuned or pinned shape (all (D, k) back to the default). */
 int sgdg_clear_tile_shapes(void);
 /* Launch statistics of one batch step: kernel launches and algorithmic bytes
