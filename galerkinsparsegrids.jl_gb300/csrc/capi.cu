@@ -29,9 +29,11 @@ void set_error(const std::string& msg) { g_err = msg; }
 
 // ------------------------------------------------------- plain form ----
 struct DeviceCSR {
-    DevBuf rowptr, col, val;
+    DevBuf rowptr, col, val, long_row, long_seg, seg_begin, seg_end, partial;
     DevCSR d{};
 };
+
+static constexpr int64_t kCsrSplit = 2048;  // entries a row group sums directly
 
 static int pick_vs(const CSR& A) {
     double avg = A.m ? double(A.nnz()) / double(A.m) : 0.0;
@@ -54,6 +56,34 @@ static std::unique_ptr<DeviceCSR> to_device(const CSR& A, cudaStream_t st) {
     D->d.col = D->col.as<int32_t>();
     D->d.val = D->val.as<double>();
     D->d.vs = pick_vs(A);
+    // long rows: segments of kCsrSplit entries
+    std::vector<int32_t> lrow, lseg(1, 0);
+    std::vector<int64_t> sb, se;
+    for (int64_t r = 0; r < A.m; r++) {
+        const int64_t b = A.rowptr[r], e = A.rowptr[r + 1];
+        if (e - b <= kCsrSplit) continue;
+        lrow.push_back((int32_t)r);
+        for (int64_t p = b; p < e; p += kCsrSplit) {
+            sb.push_back(p);
+            se.push_back(std::min(e, p + kCsrSplit));
+        }
+        lseg.push_back((int32_t)sb.size());
+    }
+    D->d.split = kCsrSplit;
+    D->d.nlong = (int64_t)lrow.size();
+    D->d.nseg = (int64_t)sb.size();
+    if (!lrow.empty()) {
+        D->long_row = upload(lrow, st);
+        D->long_seg = upload(lseg, st);
+        D->seg_begin = upload(sb, st);
+        D->seg_end = upload(se, st);
+        D->partial.alloc(sizeof(double) * sb.size());
+        D->d.long_row = D->long_row.as<int32_t>();
+        D->d.long_seg = D->long_seg.as<int32_t>();
+        D->d.seg_begin = D->seg_begin.as<int64_t>();
+        D->d.seg_end = D->seg_end.as<int64_t>();
+        D->d.partial = D->partial.as<double>();
+    }
     return D;
 }
 

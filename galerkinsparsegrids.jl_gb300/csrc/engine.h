@@ -7,6 +7,10 @@
 namespace sgdg {
 
 // ---- plain form: FP64 CSR ---------------------------------------------------
+// Rows longer than `split` entries are summed in segments of `split` by one
+// warp each (partial sums in `partial`), then combined per row in segment
+// order -- so a handful of very long rows (a coarse mode touched by every
+// coefficient) does not serialise the launch, and results stay deterministic.
 struct DevCSR {
     int64_t m;
     int64_t nnz;
@@ -14,6 +18,13 @@ struct DevCSR {
     const int32_t* col;
     const double* val;
     int vs;  // lanes per row
+    int64_t split;            // longest row a single row group sums
+    int64_t nlong, nseg;      // rows longer than split, their segments
+    const int32_t* long_row;  // nlong: the rows
+    const int32_t* long_seg;  // nlong + 1: first segment of each long row
+    const int64_t* seg_begin; // nseg + 1 style bounds: segment s is [seg_begin[s], seg_end[s])
+    const int64_t* seg_end;
+    double* partial;          // nseg
 };
 
 // ---- chosen form: matrix-free FP32 pencil apply, FP64 RK state --------------

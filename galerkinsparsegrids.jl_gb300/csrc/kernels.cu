@@ -2,7 +2,10 @@
 //
 //  * k_csr_spmv / k_csr_rk4: FP64 CSR mat-vec (the closure body *(RHS, x) of
 //    src/pdes.jl:63) with VS lanes per row; the RK4 variant fuses the
-//    classical stage combination into the row epilogue.
+//    classical stage combination into the row epilogue.  Rows longer than
+//    A.split are skipped there and summed by k_csr_segments (one warp per
+//    segment) and k_csr_long_rows (segment partials in order, then the same
+//    epilogue).
 //  * k_f64_to_f32 / k_f32_to_f64: precision conversions of whole vectors.
 #include <cuda_runtime.h>
 
@@ -12,11 +15,15 @@
 namespace sgdg {
 
 template <int VS>
-__device__ __forceinline__ double csr_row(const DevCSR& A, int64_t row, const double* __restrict__ x, int lane) {
+__device__ __forceinline__ double csr_row(const DevCSR& A, int64_t row, const double* __restrict__ x, int lane,
+                                          bool& long_row) {
     double s = 0.0;
+    long_row = false;
     if (row < A.m) {
         const int64_t b = A.rowptr[row], e = A.rowptr[row + 1];
-        for (int64_t p = b + lane; p < e; p += VS) s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
+        long_row = e - b > A.split;
+        if (!long_row)
+            for (int64_t p = b + lane; p < e; p += VS) s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
     }
 #pragma unroll
     for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -28,8 +35,9 @@ __global__ void __launch_bounds__(256) k_csr_spmv(DevCSR A, const double* __rest
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = t / VS;
     const int lane = int(t % VS);
-    double s = csr_row<VS>(A, row, x, lane);
-    if (row < A.m && lane == 0) y[row] = s;
+    bool long_row;
+    double s = csr_row<VS>(A, row, x, lane, long_row);
+    if (row < A.m && lane == 0 && !long_row) y[row] = s;
 }
 
 template <int VS>
@@ -39,8 +47,9 @@ __global__ void __launch_bounds__(256) k_csr_rk4(DevCSR A, const double* uin, do
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t row = t / VS;
     const int lane = int(t % VS);
-    double k = csr_row<VS>(A, row, uin, lane);
-    if (row < A.m && lane == 0) {
+    bool long_row;
+    double k = csr_row<VS>(A, row, uin, lane, long_row);
+    if (row < A.m && lane == 0 && !long_row) {
         double yy = y[row], aa = stage == 1 ? 0.0 : acc[row], un;
         rk_stage(stage, dt, hdt, dt6, k, yy, aa, un);
         if (stage == 4)
@@ -49,6 +58,42 @@ __global__ void __launch_bounds__(256) k_csr_rk4(DevCSR A, const double* uin, do
             acc[row] = aa;
             uout[row] = un;
         }
+    }
+}
+
+// one warp per segment of a long row
+__global__ void __launch_bounds__(256) k_csr_segments(DevCSR A, const double* __restrict__ x) {
+    const int64_t seg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (seg >= A.nseg) return;
+    double s = 0.0;
+    for (int64_t p = A.seg_begin[seg] + lane; p < A.seg_end[seg]; p += 32)
+        s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) A.partial[seg] = s;
+}
+
+// one thread per long row: its segments in order; y = A x, or the RK4 stage
+// update when acc is given
+__global__ void k_csr_long_rows(DevCSR A, double* y, double* acc, const double* uin, double* uout, double dt,
+                                double hdt, double dt6, int stage) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.nlong) return;
+    double s = 0.0;
+    for (int q = A.long_seg[i]; q < A.long_seg[i + 1]; q++) s += A.partial[q];
+    const int64_t row = A.long_row[i];
+    if (!acc) {
+        y[row] = s;
+        return;
+    }
+    double yy = y[row], aa = stage == 1 ? 0.0 : acc[row], un;
+    rk_stage(stage, dt, hdt, dt6, s, yy, aa, un);
+    if (stage == 4)
+        y[row] = yy;
+    else {
+        acc[row] = aa;
+        uout[row] = un;
     }
 }
 
@@ -89,6 +134,10 @@ cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStr
         case 16: k_csr_spmv<16><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
         default: k_csr_spmv<32><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
     }
+    if (A.nlong > 0) {
+        k_csr_segments<<<grid_for(A.nseg * 32), 256, 0, st>>>(A, x);
+        k_csr_long_rows<<<grid_for(A.nlong), 256, 0, st>>>(A, y, nullptr, nullptr, nullptr, 0.0, 0.0, 0.0, 0);
+    }
     return cudaGetLastError();
 }
 
@@ -103,6 +152,10 @@ cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double
         case 8: k_csr_rk4<8><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
         case 16: k_csr_rk4<16><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
         default: k_csr_rk4<32><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
+    }
+    if (A.nlong > 0) {
+        k_csr_segments<<<grid_for(A.nseg * 32), 256, 0, st>>>(A, uin);
+        k_csr_long_rows<<<grid_for(A.nlong), 256, 0, st>>>(A, y, acc, uin, uout, dt, hdt, dt6, stage);
     }
     return cudaGetLastError();
 }
