@@ -86,11 +86,11 @@ struct MFItem {
     int32_t rlong;     // pass: leading row blocks swept by a whole warp each
 };
 
-constexpr int kMFThreads = 128;
+constexpr int kMFThreads = 256;  // 8 warps share one copy of the operator table
 constexpr int kSpinLimit = 1 << 22;  // polls of a dependency counter before giving up
 
 // Tile shape of the pass tiles of one (D, k), chosen by the autotuner:
-// a tile has cpt * max(1, 128 / nrb) * 2^wlog columns (at least cpt; nrb =
+// a tile has cpt * max(1, kMFThreads / nrb) * 2^wlog columns (at least cpt; nrb =
 // row blocks of the pencil), and the row blocks of levels <= lmax - coop are
 // warp-cooperative.  Narrower tiles need less shared memory (more CTAs per
 // SM), wider ones amortise each item's fixed cost.

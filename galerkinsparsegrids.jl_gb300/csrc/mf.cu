@@ -310,7 +310,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     }
 }
 
-__global__ void __launch_bounds__(kMFThreads, 6)
+__global__ void __launch_bounds__(kMFThreads, 3)
     k_mf_stage(const MFItem* __restrict__ items, int nitems, const MFClass* __restrict__ classes, int* ctr, int stage,
                int in_sel, int* err, int table_bytes) {
     // dynamic shared memory: [1D operator table of the current class][tile]

@@ -188,7 +188,7 @@ int sgdg_batch_download(sgdg_batch *b, double *y_all);
  * table that every batch, server and sgdg_apply_noalloc call then uses.
  * *ntuned = number of (D, k) tuned by this call. */
 int sgdg_batch_autotune(sgdg_batch *b, int *ntuned);
-/* The tile shape used for (D, k): columns per tile = c * max(1, 128 / row
+/* The tile shape used for (D, k): columns per tile = c * max(1, 256 / row
  * blocks) * 2^wlog (at least c), row blocks of levels <= lmax - coop swept by
  * whole warps; *tuned = 1 if it came from the autotuner or
  * sgdg_set_tile_shape. */
