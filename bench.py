@@ -65,6 +65,23 @@ def parse():
     return p.parse_args()
 
 
+def max_over_ranks(x, dist, device):
+    """The maximum of a per-rank scalar over all ranks (a job takes as long as
+    its slowest rank); x itself when running alone."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank_step, steps, world, seconds):
+    """Whole-job units per second: each rank advances its own replica of the
+    workload (no exchange), so the job's units are world times one rank's."""
+    return units_per_rank_step * steps * world / seconds
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
         int(os.environ.get("LOCAL_RANK", "0"))
@@ -409,13 +426,9 @@ def run_ours(args):
     if dist:
         dist.barrier()
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     gpu_state0 = b.state(ids[0]) if rank == 0 else None
-    value = dofs_per_step * args.steps * world / (ms / 1e3)
+    value = job_rate(dofs_per_step, args.steps, world, ms / 1e3)
 
     # end to end through the C ABI with host buffers
     total = b.total_size()
@@ -429,12 +442,8 @@ def run_ours(args):
         b.upload(host.data_ptr())
         b.step(1)
         b.download(host.data_ptr())
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = dofs_per_step * args.e2e_steps * world / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e_value = job_rate(dofs_per_step, args.e2e_steps, world, e2e_s)
 
     # plain FP64 drop-in form on one solve (same problem)
     op = sg.SparseGridOperator(D, K, NLEV)
