@@ -22,8 +22,22 @@ __device__ __forceinline__ double csr_row(const DevCSR& A, int64_t row, const do
     if (row < A.m) {
         const int64_t b = A.rowptr[row], e = A.rowptr[row + 1];
         long_row = e - b > A.split;
-        if (!long_row)
-            for (int64_t p = b + lane; p < e; p += VS) s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
+        if (!long_row) {
+            // four entries per lane in flight: the column loads, then the gathers of x
+            int64_t p = b + lane;
+            for (; p + 3 * VS < e; p += 4 * VS) {
+                const int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + VS), c2 = __ldg(A.col + p + 2 * VS),
+                          c3 = __ldg(A.col + p + 3 * VS);
+                const double v0 = __ldg(A.val + p), v1 = __ldg(A.val + p + VS), v2 = __ldg(A.val + p + 2 * VS),
+                             v3 = __ldg(A.val + p + 3 * VS);
+                const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+                s = fma(v0, x0, s);
+                s = fma(v1, x1, s);
+                s = fma(v2, x2, s);
+                s = fma(v3, x3, s);
+            }
+            for (; p < e; p += VS) s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
+        }
     }
 #pragma unroll
     for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
