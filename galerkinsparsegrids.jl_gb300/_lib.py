@@ -30,7 +30,7 @@ EXPORTS = [
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
     "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
     "sgdg_server_counts",
-    "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
+    "sgdg_selftest_bounded_wait", "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
 ]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
 
@@ -96,6 +96,7 @@ def lib(build=True):
     _sig(L, "sgdg_vlasov_transform_export", [_vp, _ci, _i64p, _i32p, _f64p])
     _sig(L, "sgdg_vlasov_rhs", [_vp, _f64p, _f64p, _f64p])
     _sig(L, "sgdg_vlasov_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _f64p, _f64p])
+    _sig(L, "sgdg_selftest_bounded_wait", [ctypes.POINTER(_cd)])
     _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_server_destroy", [_vp])
     _sig(L, "sgdg_server_set_stream", [_vp, _vp])

@@ -23,6 +23,7 @@ cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double
                            int stage, cudaStream_t st);
 cudaError_t launch_vlasov_combine(const double* w, const double* p, const double* acc_in, const double* other,
                                   double* out, int64_t n, cudaStream_t st);
+cudaError_t launch_wait_selftest(const int* ctr, int need, int* err, cudaStream_t st);
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -869,6 +870,35 @@ int sgdg_batch_step_info(sgdg_batch* b, int64_t* launches, double* dofs) {
     NEED(b);
     if (launches) *launches = b->eng.launches_per_step();
     if (dofs) *dofs = b->eng.dof_updates_per_step();
+    API_END
+}
+
+int sgdg_selftest_bounded_wait(double* seconds) {
+    API_BEGIN
+    require_gpu();
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    DevBuf buf(2 * sizeof(int));
+    int err = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMemsetAsync(buf.p, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    // counter 0 must reach 1, and nothing ever increments it
+    if (e == cudaSuccess) e = launch_wait_selftest(buf.as<int>(), 1, buf.as<int>() + 1, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, buf.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) throw Error(SGDG_ECUDA, std::string("bounded wait self-test: ") + cudaGetErrorString(e));
+    if (seconds) *seconds = ms / 1e3;
+    if (!err) throw Error(SGDG_ECUDA, "bounded wait self-test: the wait did not report giving up");
+    throw Error(SGDG_ETIMEOUT, "bounded wait gave up as designed");
     API_END
 }
 

@@ -389,6 +389,17 @@ __global__ void __launch_bounds__(kMFThreads, 3)
     }
 }
 
+// Self-test of the bounded wait: thread 0 waits for a counter that nothing
+// increments; the wait gives up after kSpinLimit polls and raises *err.
+__global__ void k_wait_selftest(const int* ctr, int need, int* err) {
+    if (threadIdx.x == 0) wait_counter(ctr, need, err);
+}
+
+cudaError_t launch_wait_selftest(const int* ctr, int need, int* err, cudaStream_t st) {
+    k_wait_selftest<<<1, 32, 0, st>>>(ctr, need, err);
+    return cudaGetLastError();
+}
+
 int mf_columns_per_thread(int k) { return k <= 3 ? 4 : 2; }
 
 cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,

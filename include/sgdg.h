@@ -241,6 +241,13 @@ int sgdg_server_cancel(sgdg_server *s, int64_t request_id);
  * DOF-updates (state coefficients x RK stages) executed so far. */
 int sgdg_server_counts(sgdg_server *s, int64_t *queued, int64_t *running, int64_t *finished, double *dof_updates);
 
+/* Self-test of the device-side bounded wait the persistent kernels use for
+ * their dependencies: one thread waits for a counter that nothing increments.
+ * Returns SGDG_ETIMEOUT (the expected outcome: the wait gave up, raised the
+ * error flag and the kernel returned, leaving the context usable) and the
+ * seconds the wait took; any other status is a failure. */
+int sgdg_selftest_bounded_wait(double *seconds);
+
 /* ---- resources ---------------------------------------------------------- */
 /* Upper bound on device bytes the library may hold (0 = no limit). */
 int sgdg_set_hbm_budget(int64_t bytes);
