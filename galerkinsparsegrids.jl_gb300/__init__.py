@@ -490,10 +490,12 @@ class VlasovOperator:
 
 
 def vlasov_evolve(D, k, n, F_point, f0_modal, time0, time1, nout=2, order="rk4", scheme="sparse", dt=None,
-                  nsteps=None, op=None):
+                  nsteps=None, op=None, method="plain"):
     """vlasov_evolve (src/pdes.jl:131-227) with classical RK4 and fixed steps:
     df/dt = -(v . grad_x f) + F . grad_p f, products taken in the point basis.
-    ``F_point`` holds D arrays of point values.  Returns (times, states)."""
+    ``F_point`` holds D arrays of point values.  method "plain": assembled
+    FP64 sparse operators; "matfree": FP32 pencil sweeps, FP64 RK state.
+    Returns (times, states)."""
     _order(order)
     op = op or VlasovOperator(D, k, n, scheme)
     f0 = np.ascontiguousarray(f0_modal, np.float64)
@@ -502,8 +504,8 @@ def vlasov_evolve(D, k, n, F_point, f0_modal, time0, time1, nout=2, order="rk4",
     ns = _steps(time0, time1, dt, nsteps)
     times = np.zeros(nout)
     states = np.zeros((nout, op.N))
-    check(lib().sgdg_vlasov_evolve(op._h, op._force(F_point), f0, float(time0), float(time1), ns, int(nout), times,
-                                   states.reshape(-1)))
+    check(lib().sgdg_vlasov_evolve(op._h, op._force(F_point), f0, float(time0), float(time1), ns, int(nout),
+                                   _method(method), times, states.reshape(-1)))
     return times, list(states)
 
 
@@ -541,6 +543,14 @@ class Batch:
         i = ctypes.c_int()
         check(lib().sgdg_batch_add(self._h, kinds[kind], D, k, n, _scheme(scheme), ap, float(dt), y0,
                                    ctypes.byref(i)))
+        return i.value
+
+    def add_vlasov(self, Dx, k, n, f0, F_point, dt, scheme="sparse"):
+        """A Vlasov solve (phase space of 2 Dx dimensions, k in {2, 3, 5})."""
+        f0 = np.ascontiguousarray(f0, np.float64)
+        F = np.ascontiguousarray(np.asarray(F_point, np.float64).reshape(Dx, f0.size)).reshape(-1)
+        i = ctypes.c_int()
+        check(lib().sgdg_batch_add_vlasov(self._h, Dx, k, n, _scheme(scheme), float(dt), F, f0, ctypes.byref(i)))
         return i.value
 
     def remove(self, sid):

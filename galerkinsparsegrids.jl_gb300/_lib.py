@@ -23,6 +23,7 @@ EXPORTS = [
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
     "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info", "sgdg_batch_autotune",
+    "sgdg_batch_add_vlasov",
     "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes",
     "sgdg_transform_1d_nnz", "sgdg_transform_1d_export", "sgdg_transform_nnz", "sgdg_transform_export",
     "sgdg_vlasov_create", "sgdg_vlasov_destroy", "sgdg_vlasov_size", "sgdg_vlasov_v_point",
@@ -95,7 +96,8 @@ def lib(build=True):
     _sig(L, "sgdg_vlasov_transform_nnz", [_vp, _ci, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_vlasov_transform_export", [_vp, _ci, _i64p, _i32p, _f64p])
     _sig(L, "sgdg_vlasov_rhs", [_vp, _f64p, _f64p, _f64p])
-    _sig(L, "sgdg_vlasov_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _f64p, _f64p])
+    _sig(L, "sgdg_vlasov_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
+    _sig(L, "sgdg_batch_add_vlasov", [_vp, _ci, _ci, _ci, _ci, _cd, _f64p, _f64p, ctypes.POINTER(_ci)])
     _sig(L, "sgdg_selftest_bounded_wait", [ctypes.POINTER(_cd)])
     _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_server_destroy", [_vp])

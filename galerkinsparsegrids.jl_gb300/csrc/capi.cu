@@ -211,6 +211,25 @@ static cudaStream_t op_stream(sgdg_op* op) {
     return op->stream;
 }
 
+// Point weights of the matrix-free Vlasov right-hand side: term d < Dx is
+// -v_d .* (x-derivative), term Dx + d is F_d .* (p-derivative); each weight as
+// an FP32 (hi, lo) pair (a rounded weight would perturb the operator
+// systematically).  Layout: hi of all 2 Dx terms, then lo.
+static std::vector<float> vlasov_weights(const SparseIndex& ix, int Dx, const double* F) {
+    const int64_t N = ix.N;
+    const int P = 2 * Dx;
+    const std::vector<double> v = vlasov_velocity_points(ix, Dx);
+    std::vector<float> w((size_t)2 * P * N);
+    for (int t = 0; t < P; t++)
+        for (int64_t e = 0; e < N; e++) {
+            const double x = t < Dx ? -v[(size_t)t * N + e] : F[(size_t)(t - Dx) * N + e];
+            const float hi = (float)x;
+            w[(size_t)t * N + e] = hi;
+            w[((size_t)P + t) * N + e] = (float)(x - (double)hi);
+        }
+    return w;
+}
+
 // nodal transforms: the D-dimensional restricted Kronecker product of a 1D map
 static CSR build_transform(int D, int k, int n, int scheme, int which) {
     if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
@@ -680,13 +699,40 @@ int sgdg_vlasov_rhs(sgdg_vlasov* v, const double* F_point, const double* f, doub
 }
 
 int sgdg_vlasov_evolve(sgdg_vlasov* v, const double* F_point, const double* f0, double t0, double t1, int64_t nsteps,
-                       int nout, double* times, double* states) {
+                       int nout, int method, double* times, double* states) {
     API_BEGIN
     NEED(v);
     NEED(F_point);
     NEED(f0);
     NEED(states);
     check_evolve_args(nsteps, nout, t0, t1);
+    if (method == SGDG_METHOD_MATFREE) {
+        if (!v->stream) {
+            require_gpu();
+            CK(cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking));
+        }
+        MFEngine eng(v->stream);
+        SolveSpec sp{};
+        sp.kind = MF_KIND_VLASOV;
+        sp.D = v->P;
+        sp.k = v->k;
+        sp.n = v->n;
+        sp.scheme = v->ix.scheme;
+        sp.dt = (t1 - t0) / double(nsteps);
+        sp.apply_dim = -1;
+        const std::vector<float> w = vlasov_weights(v->ix, v->D, F_point);
+        const int id = eng.add(sp, f0, w.data());
+        auto steps = out_steps(nsteps, nout);
+        int64_t done = 0;
+        for (int i = 0; i < nout; i++) {
+            eng.step(steps[i] - done);
+            done = steps[i];
+            eng.get_state(id, states + (size_t)i * v->ix.N);
+            if (times) times[i] = t0 + (t1 - t0) * double(steps[i]) / double(nsteps);
+        }
+        return SGDG_OK;
+    }
+    if (method != SGDG_METHOD_PLAIN) throw Error(SGDG_EINVAL, "method must be PLAIN (0) or MATFREE (1)");
     v->to_gpu();
     cudaStream_t st = v->stream;
     const int64_t N = v->ix.N;
@@ -800,6 +846,29 @@ int sgdg_set_tile_shape(int D, int k, int wlog, int coop) {
 int sgdg_clear_tile_shapes(void) {
     API_BEGIN
     mf_clear_tiles();
+    API_END
+}
+
+int sgdg_batch_add_vlasov(sgdg_batch* b, int Dx, int k, int n, int scheme, double dt, const double* F_point,
+                          const double* f0, int* id) {
+    API_BEGIN
+    NEED(b);
+    NEED(F_point);
+    NEED(f0);
+    NEED(id);
+    if (Dx < 1 || 2 * Dx > 8) throw Error(SGDG_EINVAL, "Dx (space dimensions) must be 1..4");
+    if (!std::isfinite(dt)) throw Error(SGDG_EINVAL, "dt must be finite");
+    SolveSpec sp{};
+    sp.kind = MF_KIND_VLASOV;
+    sp.D = 2 * Dx;
+    sp.k = k;
+    sp.n = n;
+    sp.scheme = scheme;
+    sp.dt = dt;
+    sp.apply_dim = -1;
+    const SparseIndex ix = make_index(sp.D, k, n, scheme);
+    const std::vector<float> w = vlasov_weights(ix, Dx, F_point);
+    *id = b->eng.add(sp, f0, w.data());
     API_END
 }
 

@@ -161,22 +161,25 @@ std::shared_ptr<const DLF1D> dlf1d(int k, int n) {
 
 namespace sgdg {
 
-MFOperator mf_operator(int k, int n) {
-    auto op = dlf1d(k, n);
+// Block table of a 1D operator in block-CSR form (k x k blocks over the 2^n
+// (level, cell) blocks): blocks whose entries are all below prune * (largest
+// entry) are dropped, and blocks equal to 1e-12 of the largest entry share
+// one table entry (they are the same block up to the roundoff of their
+// separate evaluation).
+static MFOperator mf_table(int k, int n, int nblocks, const std::vector<int32_t>& rowptr,
+                           const std::vector<int32_t>& colblk, const std::vector<double>& val, double prune) {
     MFOperator M;
     M.k = k;
     M.n = n;
     M.rs = ((2 * k + 3) / 4) * 4;
     double vmax = 0.0;
-    for (double v : op->val) vmax = std::max(vmax, std::fabs(v));
-    const double drop = 1e-10 * vmax;
-    // blocks equal to 1e-12 of vmax share one table entry (they are the same
-    // block up to the roundoff of their separate evaluation)
+    for (double v : val) vmax = std::max(vmax, std::fabs(v));
+    const double drop = prune * vmax;
     std::map<std::vector<long long>, int> ids;
-    M.rowptr.assign(op->nblocks + 1, 0);
-    for (int rb = 0; rb < op->nblocks; rb++) {
-        for (int p = op->rowptr[rb]; p < op->rowptr[rb + 1]; p++) {
-            const double* b = &op->val[(size_t)p * k * k];
+    M.rowptr.assign(nblocks + 1, 0);
+    for (int rb = 0; rb < nblocks; rb++) {
+        for (int p = rowptr[rb]; p < rowptr[rb + 1]; p++) {
+            const double* b = &val[(size_t)p * k * k];
             double bmax = 0.0;
             for (int t = 0; t < k * k; t++) bmax = std::max(bmax, std::fabs(b[t]));
             if (bmax <= drop) continue;
@@ -199,13 +202,47 @@ MFOperator mf_operator(int k, int n) {
             } else {
                 id = it->second;
             }
-            if (id >= 4096 || op->colblk[p] >= (1 << 19))
+            if (id >= 4096 || colblk[p] >= (1 << 19))
                 throw Error(7, "1D operator too large for the matrix-free block table");
-            M.ent.push_back((op->colblk[p] << 12) | id);
+            M.ent.push_back((colblk[p] << 12) | id);
         }
         M.rowptr[rb + 1] = (int32_t)M.ent.size();
     }
     return M;
+}
+
+MFOperator mf_operator(int k, int n) {
+    auto op = dlf1d(k, n);
+    // the vanishing moments make fine x coarse blocks away from the coarse
+    // function's breakpoints exact zeros, stored as roundoff (<= 1e-14 of the
+    // largest entry; genuine entries are >= 7e-3 of it)
+    return mf_table(k, n, op->nblocks, op->rowptr, op->colblk, op->val, 1e-10);
+}
+
+MFOperator mf_transform_table(int k, int n, int which) {
+    // element CSR of the 1D map -> dense k x k blocks per (level, cell) pair
+    const CSR T = transform_1d(k, n, which);
+    const int nb = 1 << n;
+    std::vector<int32_t> rowptr(nb + 1, 0), colblk;
+    std::vector<double> val;
+    for (int rb = 0; rb < nb; rb++) {
+        std::map<int, std::vector<double>> blocks;  // column block -> k x k
+        for (int i = 0; i < k; i++) {
+            const int64_t row = (int64_t)rb * k + i;
+            for (int64_t p = T.rowptr[row]; p < T.rowptr[row + 1]; p++) {
+                const int cb = T.col[p] / k, j = T.col[p] % k;
+                auto& bl = blocks[cb];
+                if (bl.empty()) bl.assign((size_t)k * k, 0.0);
+                bl[(size_t)i * k + j] = T.val[p];
+            }
+        }
+        for (auto& e : blocks) {
+            colblk.push_back(e.first);
+            val.insert(val.end(), e.second.begin(), e.second.end());
+        }
+        rowptr[rb + 1] = (int32_t)colblk.size();
+    }
+    return mf_table(k, n, nb, rowptr, colblk, val, 0.0);
 }
 
 }  // namespace sgdg

@@ -36,9 +36,13 @@ struct DevCSR {
 // tiles: sweep the 1D operator, accumulate into rhs); the last pass applies the
 // RK stage update to the elements it completes.  Each phase waits for the
 // previous phase of its group.
-enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1 };
-enum : int { TILE_FIRST = 1, TILE_LAST = 2, TILE_RK = 4 };  // TILE_RK: last pass with the RK4 update fused
-enum : int { ITEM_PASS = 0 };
+enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1, MF_KIND_VLASOV = 2 };
+// TILE_RK: the pass completes the right-hand side and applies the RK4 update;
+// TILE_STORE: the result goes to a scratch vector; TILE_WACC: times a point
+// weight, added into the point-basis accumulator; TILE_WAIT_IN: the input
+// was written by the previous phase of this launch (wait before gathering).
+enum : int { TILE_FIRST = 1, TILE_LAST = 2, TILE_RK = 4, TILE_STORE = 8, TILE_WACC = 16, TILE_WAIT_IN = 32 };
+enum : int { TABLE_DERIVATIVE = -1 };  // MFItem::tab; 0..3: the nodal transforms
 
 struct MFClass {
     const int32_t* s_rowptr;  // 1D operator, block CSR over 2^n row blocks (2^n + 1 entries)
@@ -56,6 +60,13 @@ struct MFClass {
     int32_t D, k, kD, kind, rs;
     int32_t s_nrow, s_nent, s_nval;  // table sizes (ints, ints, floats) for the shared-memory copy
     int32_t s_shared;                // 1: pass tiles read a shared-memory copy of the table; 0: global memory
+    // Vlasov classes: the four nodal transforms (1D block tables, read through
+    // L1), scratch vectors and the point weights of the D point products
+    const int32_t* t_rowptr[4];
+    const int32_t* t_ent[4];
+    const float* t_val[4];
+    float* vb[3];             // per slot N: two ping-pong vectors and the point-basis accumulator
+    const float* vw;          // per slot 2 x D x N: weight of term d at [d N] (hi) and [(D + d) N] (lo)
 };
 
 // bytes of the shared-memory copy of a class's 1D operator table
@@ -67,10 +78,14 @@ inline int mf_table_bytes(int nrow, int nent, int nval) {
 constexpr int kMFTableSmemMax = 48 * 1024;
 
 struct MFItem {
-    int16_t type;      // ITEM_PASS
+    int16_t tab;       // 1D table: TABLE_DERIVATIVE or a nodal transform 0..3
     int16_t cls;
-    int16_t d;         // pass: 0-based dimension
-    int16_t flags;     // pass: TILE_FIRST | TILE_LAST | TILE_RK
+    int16_t d;         // 0-based dimension of the pencils
+    int16_t flags;     // TILE_*
+    int16_t src;       // input: -1 the stage input, 0..2 a scratch vector
+    int16_t dst;       // TILE_STORE / TILE_WACC output vector
+    int16_t wsel;      // TILE_WACC: the weight (term) index
+    int16_t pad;
     int32_t wait_ctr;  // counter to wait for (-1: none) ...
     int32_t wait_need; // ... until it reaches this value
     int32_t done_ctr;  // counter incremented when the item is done

@@ -208,22 +208,35 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             cb[j] = 0;
         }
     }
+    // an input written by the previous phase of this launch must be complete
+    if ((it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
     const TileCols cols{cslot, ca, cb};
-    // gather the stage input (written by the previous launch) into X
     const float* __restrict__ uin = C.u[in_sel];
     const int ne = m << lw;
-    for (int e = tid; e < ne; e += kMFThreads) {
-        const int row = e >> lw, j = e & (W - 1);
-        const int s = cslot[j];
-        if (s < 0) {
-            X[e] = 0.f;
-            continue;
+    if (it.src < 0) {
+        // gather the stage input (written by the previous launch) into X
+        for (int e = tid; e < ne; e += kMFThreads) {
+            const int row = e >> lw, j = e & (W - 1);
+            const int s = cslot[j];
+            if (s < 0) {
+                X[e] = 0.f;
+                continue;
+            }
+            const int rb = row / K, i = row - rb * K;
+            cp_async4(X + e, uin + (size_t)s * C.Ns + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j));
         }
-        const int rb = row / K, i = row - rb * K;
-        cp_async4(X + e, uin + (size_t)s * C.Ns + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j));
+        cp_async_wait_all();
+    } else {
+        // a scratch vector written in this launch by other SMs: L2 loads (.cg)
+        const float* __restrict__ vin = C.vb[it.src];
+        for (int e = tid; e < ne; e += kMFThreads) {
+            const int row = e >> lw, j = e & (W - 1);
+            const int s = cslot[j];
+            const int rb = row / K, i = row - rb * K;
+            X[e] = s < 0 ? 0.f : __ldcg(vin + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j));
+        }
     }
-    cp_async_wait_all();
     __syncthreads();
     const int lwq = lw - (CPT == 4 ? 2 : 1);
     const int rlong = it.rlong;  // row blocks of levels <= lmax - coop (tile shape)
@@ -247,9 +260,31 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     }
     apply_rows<K, CPT>(T, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Z, rb, jq, o); });
     // the partial sums of this group's previous pass must be complete
-    if (it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
+    if (!(it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
     const bool first = (it.flags & TILE_FIRST) != 0;
+    if (it.flags & (TILE_STORE | TILE_WACC)) {
+        // Vlasov: a transform's result to a scratch vector, or the point
+        // product w_d .* result added into the point-basis accumulator
+        float* __restrict__ out = C.vb[it.dst];
+        const bool wacc = (it.flags & TILE_WACC) != 0;
+        for (int e = tid; e < ne; e += kMFThreads) {
+            const int row = e >> lw, j = e & (W - 1);
+            const int s = cslot[j];
+            if (s < 0) continue;
+            const int rb = row / K, i = row - rb * K;
+            const int off = elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
+            float* op = out + (size_t)s * C.N + off;
+            float v = Z[e];
+            if (wacc) {
+                const float* wp = C.vw + (size_t)s * 2 * C.D * C.N + (size_t)it.wsel * C.N + off;
+                v = fmaf(__ldg(wp), v, __ldg(wp + (size_t)C.D * C.N) * v);
+                if (!first) v += __ldcg(op);
+            }
+            __stcg(op, v);
+        }
+        return;
+    }
     if (!(it.flags & TILE_RK)) {
         // partial sum sum_{q <= d} coef_q D_q u of this tile's elements
         for (int e = tid; e < ne; e += kMFThreads) {
@@ -354,7 +389,9 @@ __global__ void __launch_bounds__(kMFThreads, 3)
         if (tid == 0) s_cls_id = it.cls;  // read again only after the next barrier
         if (tid < it.lmax) s_off[tid] = (int)C.blockoff[it.boff + tid];  // seen after pass_tile's first barrier
         OpTable T{C.s_rowptr, C.s_ent, C.s_val};
-        if (C.s_shared) {
+        if (it.tab != TABLE_DERIVATIVE) {  // a nodal transform: read through L1
+            T = OpTable{C.t_rowptr[it.tab], C.t_ent[it.tab], C.t_val[it.tab]};
+        } else if (C.s_shared) {
             int* trow = reinterpret_cast<int*>(smem);
             int* tent = trow + C.s_nrow;
             float* tval = smem + (((C.s_nrow + C.s_nent) * 4 + 15) / 16) * 4;
@@ -368,7 +405,7 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             }
             T = OpTable{trow, tent, tval};
         }
-        switch (C.k * 2 + C.kind) {
+        switch (C.k * 2 + (C.kind == MF_KIND_WAVE ? 1 : 0)) {  // Vlasov sweeps once, like advection
             case 2: pass_tile<1, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
             case 3: pass_tile<1, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
             case 4: pass_tile<2, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;

@@ -50,10 +50,15 @@ const MFEngine::Solve& MFEngine::at(int id) const {
 
 bool MFEngine::live(int id) const { return id >= 0 && id < (int)solves_.size() && solves_[id].live; }
 
-int MFEngine::add(const SolveSpec& sp, const double* y0) {
+int MFEngine::add(const SolveSpec& sp, const double* y0, const float* weights) {
     require_gpu();
     if (sp.k < 1 || sp.k > 5) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports 1 <= k <= 5 (use the plain form)");
     if (sp.D > 8) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports D <= 8");
+    if (sp.kind == MF_KIND_VLASOV) {
+        if (sp.apply || sp.D % 2 != 0) throw Error(SGDG_EINVAL, "a Vlasov solve has an even phase-space dimension");
+        if (sp.k != 2 && sp.k != 3 && sp.k != 5) throw Error(SGDG_EINVAL, "the nodal basis exists for k = 2, 3, 5");
+        if (!weights) throw Error(SGDG_EINVAL, "a Vlasov solve needs its point weights");
+    }
     Solve s;
     s.spec = sp;
     SparseIndex ix = make_index(sp.D, sp.k, sp.n, sp.scheme);
@@ -61,7 +66,7 @@ int MFEngine::add(const SolveSpec& sp, const double* y0) {
     s.N = ix.N;
     s.Ns = sp.kind == MF_KIND_WAVE && !sp.apply ? 2 * ix.N : ix.N;
     // admission: the solve's arena share must fit the HBM budget now
-    const int64_t need = solve_bytes(s.N, s.Ns);
+    const int64_t need = solve_bytes(s.N, s.Ns, sp.kind, sp.D);
     const int64_t budget = g_budget.load();
     const int64_t held = g_in_use.load() - dead_bytes() + pending_bytes_;
     if (budget > 0 && held + need > budget)
@@ -69,21 +74,23 @@ int MFEngine::add(const SolveSpec& sp, const double* y0) {
                                             std::to_string(held) + " of " + std::to_string(budget) + " committed");
     if (y0) s.pending.assign(y0, y0 + s.Ns);
     else s.pending.assign(s.Ns, 0.0);
+    if (sp.kind == MF_KIND_VLASOV) s.weights.assign(weights, weights + (size_t)2 * sp.D * s.N);
     solves_.push_back(std::move(s));
     pending_bytes_ += need;
     dirty_ = true;
     return (int)solves_.size() - 1;
 }
 
-int64_t MFEngine::solve_bytes(int64_t N, int64_t Ns) {
-    // y, acc (FP64), two stage inputs (FP32), partial sums (FP32)
-    return Ns * (8 + 8 + 4 + 4) + N * 4;
+int64_t MFEngine::solve_bytes(int64_t N, int64_t Ns, int kind, int D) {
+    // y, acc (FP64), two stage inputs (FP32), partial sums (FP32); Vlasov:
+    // three scratch vectors and 2 D point weights (FP32)
+    return Ns * (8 + 8 + 4 + 4) + N * 4 + (kind == MF_KIND_VLASOV ? N * 4 * (3 + 2 * (int64_t)D) : 0);
 }
 
 int64_t MFEngine::dead_bytes() const {
     int64_t b = 0;
     for (auto& s : solves_)
-        if (!s.live && s.cls >= 0) b += solve_bytes(s.N, s.Ns);
+        if (!s.live && s.cls >= 0) b += solve_bytes(s.N, s.Ns, s.spec.kind, s.spec.D);
     return b;
 }
 
@@ -140,6 +147,24 @@ const MFEngine::STable& MFEngine::stab(int k, int n) {
     S.nval = (int)M.val.size();
     CK(cudaStreamSynchronize(stream_));
     return stabs_.emplace(key, std::move(S)).first->second;
+}
+
+const MFEngine::TTables& MFEngine::ttab(int k, int n) {
+    auto key = std::make_pair(k, n);
+    auto it = ttabs_.find(key);
+    if (it != ttabs_.end()) return it->second;
+    TTables T;
+    for (int w = 0; w < 4; w++) {
+        const MFOperator M = mf_transform_table(k, n, w);
+        T.t[w].rowptr = upload(M.rowptr, stream_);
+        T.t[w].ent = upload(M.ent, stream_);
+        T.t[w].val = upload(M.val, stream_);
+        T.t[w].nrow = (int)M.rowptr.size();
+        T.t[w].nent = (int)M.ent.size();
+        T.t[w].nval = (int)M.val.size();
+    }
+    CK(cudaStreamSynchronize(stream_));
+    return ttabs_.emplace(key, std::move(T)).first->second;
 }
 
 void MFEngine::plan() {
@@ -213,6 +238,16 @@ void MFEngine::plan() {
         c.u0.alloc(sizeof(float) * ns * c.Ns);
         c.u1.alloc(sizeof(float) * ns * c.Ns);
         c.rhs.alloc(sizeof(float) * ns * c.N);
+        const bool vlasov = s0.spec.kind == MF_KIND_VLASOV;
+        if (vlasov) {
+            c.vb.alloc(sizeof(float) * 3 * ns * c.N);
+            c.vw.alloc(sizeof(float) * 2 * (size_t)D * ns * c.N);
+            for (int sl = 0; sl < ns; sl++) {
+                const Solve& s = solves_[c.slots[sl]];
+                CK(cudaMemcpyAsync(c.vw.as<float>() + (size_t)sl * 2 * D * c.N, s.weights.data(),
+                                   sizeof(float) * s.weights.size(), cudaMemcpyHostToDevice, stream_));
+            }
+        }
         std::vector<double> dt(3 * (size_t)ns);
         std::vector<float> coef((size_t)ns * 16, 0.f);
         std::vector<int32_t> status(ns, 0);
@@ -224,7 +259,8 @@ void MFEngine::plan() {
             for (int d = 0; d < 8; d++) {
                 // factor on D_d as an FP32 (hi, lo) pair: a rounded velocity
                 // would perturb the operator systematically
-                const double f = s.spec.apply || s.spec.kind == MF_KIND_WAVE ? 1.0 : -s.spec.a[d];
+                const double f =
+                    s.spec.apply || s.spec.kind == MF_KIND_WAVE || s.spec.kind == MF_KIND_VLASOV ? 1.0 : -s.spec.a[d];
                 coef[sl * 16 + d] = (float)f;
                 coef[sl * 16 + 8 + d] = (float)(f - (double)(float)f);
             }
@@ -295,6 +331,16 @@ void MFEngine::plan() {
         m.kD = kD;
         m.kind = s0.spec.kind;
         m.rs = ((2 * m.k + 3) / 4) * 4;
+        if (m.kind == MF_KIND_VLASOV) {
+            const TTables& T = ttab(m.k, s0.spec.n);
+            for (int w = 0; w < 4; w++) {
+                m.t_rowptr[w] = T.t[w].rowptr.as<int32_t>();
+                m.t_ent[w] = T.t[w].ent.as<int32_t>();
+                m.t_val[w] = T.t[w].val.as<float>();
+            }
+            for (int b = 0; b < 3; b++) m.vb[b] = c.vb.as<float>() + (size_t)b * c.slots.size() * c.N;
+            m.vw = c.vw.as<float>();
+        }
         ch.push_back(m);
     }
     std::vector<MFItem> items;
@@ -354,8 +400,8 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
         for (int s0 = 0; s0 < ns; s0 += gs) {
             const int s1 = std::min(ns, s0 + gs);
             Group grp;
-            for (size_t ph = 0; ph < dims.size(); ph++) {
-                const int d = dims[ph];
+            // one phase: tiles of every pencil along d over the group's slots
+            auto phase = [&](int d, int tab, int src, int dst, int flags, int wsel) {
                 int kd1 = 1;
                 for (int q = 0; q < d; q++) kd1 *= k;
                 std::vector<MFItem> list;
@@ -369,13 +415,13 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                     smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
                     for (int64_t g0 = cbeg; g0 < cend; g0 += Wp) {
                         MFItem it{};
-                        it.type = ITEM_PASS;
+                        it.tab = (int16_t)tab;
                         it.cls = (int16_t)ci;
                         it.d = (int16_t)d;
-                        const bool last = ph + 1 == dims.size();
-                        // the last pass updates the RK state (never while tuning: no state changes)
-                        it.flags = (int16_t)((ph == 0 ? TILE_FIRST : 0) | (last ? TILE_LAST : 0) |
-                                             (last && !sp.apply && !pass_only ? TILE_RK : 0));
+                        it.flags = (int16_t)flags;
+                        it.src = (int16_t)src;
+                        it.dst = (int16_t)dst;
+                        it.wsel = (int16_t)wsel;
                         it.lmax = p.lmax;
                         it.lp = p.lp;
                         it.boff = c.boff_index[bi + pi];
@@ -390,6 +436,43 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                     }
                 }
                 grp.phases.push_back(std::move(list));
+            };
+            // the RK state is never updated while tuning (no state changes)
+            const int rk = !sp.apply && !pass_only ? TILE_RK : 0;
+            if (sp.kind != MF_KIND_VLASOV) {
+                // one pass per dimension accumulating into rhs; the last applies the RK update
+                for (size_t ph = 0; ph < dims.size(); ph++) {
+                    const bool last = ph + 1 == dims.size();
+                    phase(dims[ph], TABLE_DERIVATIVE, -1, 0,
+                          (ph == 0 ? TILE_FIRST : 0) | (last ? TILE_LAST | rk : 0), 0);
+                }
+            } else {
+                // Vlasov right-hand side (src/pdes.jl:174-192) as sweeps: for each
+                // phase dimension d, D_d then the modal->nodal and nodal->points
+                // transforms (one sweep per dimension each; the restricted
+                // Kronecker products factor exactly because the 1D maps are
+                // level-triangular), times the point weight of d into the
+                // accumulator; then points->nodal and nodal->modal, whose last
+                // sweep applies the RK update.  Every phase after the first reads
+                // what the previous phase wrote.
+                const int P = D, A = 0, ACC = 2;
+                for (int d = 0; d < P; d++) {
+                    phase(d, TABLE_DERIVATIVE, -1, A, TILE_STORE | (d > 0 ? TILE_WAIT_IN : 0), 0);
+                    int cur = A;
+                    for (int q = 0; q < P; q++, cur ^= 1)
+                        phase(q, TRANSFORM_MODAL_TO_NODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
+                    for (int q = 0; q < P - 1; q++, cur ^= 1)
+                        phase(q, TRANSFORM_NODAL_TO_POINTS, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
+                    phase(P - 1, TRANSFORM_NODAL_TO_POINTS, cur, ACC,
+                          TILE_WACC | TILE_WAIT_IN | (d == 0 ? TILE_FIRST : 0), d);
+                }
+                phase(0, TRANSFORM_POINTS_TO_NODAL, ACC, A, TILE_STORE | TILE_WAIT_IN, 0);
+                int cur = A;
+                for (int q = 1; q < P; q++, cur ^= 1)
+                    phase(q, TRANSFORM_POINTS_TO_NODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
+                for (int q = 0; q < P - 1; q++, cur ^= 1)
+                    phase(q, TRANSFORM_NODAL_TO_MODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
+                phase(P - 1, TRANSFORM_NODAL_TO_MODAL, cur, 0, TILE_FIRST | TILE_LAST | rk | TILE_WAIT_IN, 0);
             }
             groups.push_back(std::move(grp));
         }

@@ -14,8 +14,8 @@
 namespace sgdg {
 
 struct SolveSpec {
-    int kind = MF_KIND_ADVECT;  // MF_KIND_ADVECT / MF_KIND_WAVE
-    int D = 0, k = 0, n = 0, scheme = 0;
+    int kind = MF_KIND_ADVECT;  // MF_KIND_ADVECT / MF_KIND_WAVE / MF_KIND_VLASOV
+    int D = 0, k = 0, n = 0, scheme = 0;  // Vlasov: D = phase-space dimensions
     double a[8] = {0};          // advection velocity
     double dt = 0.0;
     bool apply = false;         // operator application only (no RK): result in rhs
@@ -32,8 +32,9 @@ class MFEngine {
     void set_stream(cudaStream_t st);
     cudaStream_t stream() const { return stream_; }
 
-    // Adds a solve; y0 (host, Ns values) may be null (zero state).
-    int add(const SolveSpec& sp, const double* y0);
+    // Adds a solve; y0 (host, Ns values) may be null (zero state).  A Vlasov
+    // solve also takes its point weights: 2 x D x N floats (hi block, lo block)
+    int add(const SolveSpec& sp, const double* y0, const float* weights = nullptr);
     void remove(int id);
     void cancel(int id);  // freezes the solve's state (its RK updates are skipped)
     bool live(int id) const;
@@ -56,7 +57,7 @@ class MFEngine {
     double dof_updates_per_step() const;
     int64_t launches_per_step() const { return 4; }
     int check_error();  // returns SGDG_OK or SGDG_ETIMEOUT after a bounded wait gave up
-    static int64_t solve_bytes(int64_t N, int64_t Ns);  // device bytes a solve occupies
+    static int64_t solve_bytes(int64_t N, int64_t Ns, int kind = MF_KIND_ADVECT, int D = 0);  // device bytes of a solve
     int64_t pending_bytes() const { return pending_bytes_; }
     int64_t dead_bytes() const;  // arena shares of removed solves, freed by the next re-plan
     // device bytes a re-plan holds on top of the steady state: the largest
@@ -70,10 +71,14 @@ class MFEngine {
         int cls = -1, slot = -1;
         bool live = true, cancelled = false;
         std::vector<double> pending;  // host state not yet on the device
+        std::vector<float> weights;   // Vlasov point weights (kept on the host for re-plans)
     };
     struct STable {
         DevBuf rowptr, ent, val;
         int nrow = 0, nent = 0, nval = 0;
+    };
+    struct TTables {  // the four nodal transforms of one (k, n)
+        STable t[4];
     };
     struct ClassArena {
         std::tuple<int, int, int, int, int, bool, int> key;
@@ -83,12 +88,14 @@ class MFEngine {
         int64_t N = 0, Ns = 0;
         std::vector<int> slots;                    // solve id per slot
         DevBuf y, acc, u0, u1, rhs, dt, coef, status, blockoff;
+        DevBuf vb, vw;  // Vlasov: 3 scratch vectors per slot, point weights per slot
     };
 
     void plan();
     void build_items(std::vector<MFItem>& items, int& nctr, bool pass_only = false,
                      const std::map<std::pair<int, int>, MFTile>* shapes = nullptr);
     const STable& stab(int k, int n);
+    const TTables& ttab(int k, int n);
     void capture();
     void drop_graph();
     Solve& at(int id);
@@ -98,6 +105,7 @@ class MFEngine {
     std::vector<Solve> solves_;
     std::vector<std::unique_ptr<ClassArena>> classes_;
     std::map<std::pair<int, int>, STable> stabs_;
+    std::map<std::pair<int, int>, TTables> ttabs_;
     DevBuf classes_d_, items_d_, ctr_d_, err_d_;
     int nitems_ = 0, nctr_ = 0, grid_ = 0;
     int64_t pending_bytes_ = 0;  // admitted but not yet allocated

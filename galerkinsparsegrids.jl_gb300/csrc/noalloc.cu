@@ -144,7 +144,8 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                 smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
                 for (int64_t g0 = 0; g0 < p.R; g0 += Wp) {
                     MFItem it{};
-                    it.type = ITEM_PASS;
+                    it.tab = TABLE_DERIVATIVE;
+                    it.src = -1;  // the stage input
                     it.cls = 0;
                     it.d = (int16_t)d;
                     it.flags = (int16_t)((ph == 0 ? TILE_FIRST : 0) | (ph + 1 == dims.size() ? TILE_LAST : 0));

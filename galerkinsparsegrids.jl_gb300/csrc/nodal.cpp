@@ -489,4 +489,40 @@ CSR transform_dd(const SparseIndex& ix, const CSR& T1) {
     return R;
 }
 
+// Collocation point of the 1D point-basis index (level L, cell c, mode m,
+// 1-based): the k-1 new nodes of the cell, then its last point
+// (src/1d_nodal_basis.jl:183-213).
+double nodal_point(int k, int L, int c, int m) {
+    const int l = L - 1;
+    const double nc = (double)(1 << (l > 1 ? l - 1 : 0));
+    if (m < k) {
+        const double node = l == 0 ? double(m - 1) / (k - 1) : (2.0 * (m - 1) + 1) / (2.0 * (k - 1));
+        return (double(c - 1) + node) / nc;
+    }
+    return l == 0 ? 1.0 : (double(c) - 0.5) / nc;
+}
+
+// v_d = 2 p_d - 1 at every point of the phase-space grid (d = 0..Dx-1, p_d =
+// phase dimension Dx + d): the velocity points of src/pdes.jl:166-172, which
+// n2p m2n of the exact modal coefficients reproduce to roundoff.
+std::vector<double> vlasov_velocity_points(const SparseIndex& ix, int Dx) {
+    const int D = ix.D, k = ix.k;
+    std::vector<double> out((size_t)Dx * ix.N);
+    int64_t e = 0;
+    for (int t = 0; t < ix.nlev; t++) {
+        const int* L = &ix.levels[(size_t)t * D];
+        for (int64_t cc = 0; cc < ix.lev_cells[t]; cc++)
+            for (int64_t mm = 0; mm < ix.kD; mm++, e++) {
+                int64_t r = cc, s = mm;
+                for (int q = 0; q < D; q++) {
+                    const int c = int(r % ncells(L[q])) + 1, m = int(s % k) + 1;
+                    r /= ncells(L[q]);
+                    s /= k;
+                    if (q >= Dx) out[(size_t)(q - Dx) * ix.N + e] = 2.0 * nodal_point(k, L[q], c, m) - 1.0;
+                }
+            }
+    }
+    return out;
+}
+
 }  // namespace sgdg

@@ -83,7 +83,8 @@ struct MFOperator {
     std::vector<int32_t> ent;     // per row, sorted by column block
     std::vector<float> val;       // ndist blocks of k rows x rs floats
 };
-MFOperator mf_operator(int k, int n);
+MFOperator mf_operator(int k, int n);                  // the 1D derivative, pruned
+MFOperator mf_transform_table(int k, int n, int which);  // a nodal transform (see below)
 
 // ------------------------------------------------------------ index map ----
 // Sparse-grid coefficient layout of src/dg_vmethods.jl:102-142: level tuples
@@ -128,6 +129,8 @@ enum : int {
 };
 CSR transform_1d(int k, int n, int which);                  // transform_1D
 CSR transform_dd(const SparseIndex& ix, const CSR& T1);      // transform(D, k, n, mat_1D)
+double nodal_point(int k, int L, int c, int m);                // collocation point of a point-basis index
+std::vector<double> vlasov_velocity_points(const SparseIndex& ix, int Dx);  // 2 p_d - 1, Dx x N
 
 // ------------------------------------------------------ pencil schedule ----
 // A pencil for dimension d fixes the levels of every other dimension; its

@@ -147,9 +147,12 @@ int sgdg_vlasov_transform_export(const sgdg_vlasov *v, int which, int64_t *rowpt
  * force F_point (D x N, point basis), FP64 on the GPU. */
 int sgdg_vlasov_rhs(sgdg_vlasov *v, const double *F_point, const double *f, double *out);
 /* Classical RK4 with nsteps fixed steps on [t0, t1]; nout >= 2 equally spaced
- * states (the first is f0), FP64 sparse operators on the GPU. */
+ * states (the first is f0).  SGDG_METHOD_PLAIN: the assembled FP64 sparse
+ * operators; SGDG_METHOD_MATFREE: pencil sweeps of the derivative and of the
+ * four transforms in FP32 (operators and weights as hi/lo FP32 pairs), FP64
+ * RK state. */
 int sgdg_vlasov_evolve(sgdg_vlasov *v, const double *F_point, const double *f0, double t0, double t1, int64_t nsteps,
-                       int nout, double *times, double *states);
+                       int nout, int method, double *times, double *states);
 
 /* ---- batches of independent solves (matrix-free form) ------------------- */
 /* Many solves of uneven D, k, n advance together: each RK stage is one
@@ -162,6 +165,10 @@ int sgdg_batch_destroy(sgdg_batch *b);
  * a[D] is the advection velocity (ignored for the wave).  Returns its id. */
 int sgdg_batch_add(sgdg_batch *b, int kind, int D, int k, int n, int scheme, const double *a, double dt,
                    const double *y0, int *id);
+/* Adds a Vlasov solve (matrix-free form): Dx space dimensions (phase space
+ * 2 Dx, k in {2, 3, 5}), force F_point (Dx x N, point basis), modal f0 (N). */
+int sgdg_batch_add_vlasov(sgdg_batch *b, int Dx, int k, int n, int scheme, double dt, const double *F_point,
+                          const double *f0, int *id);
 /* Removes a solve and frees its device state (ids of others are unchanged). */
 int sgdg_batch_remove(sgdg_batch *b, int id);
 /* Use a caller stream (cudaStream_t) for all work of this batch. */

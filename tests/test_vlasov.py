@@ -108,3 +108,37 @@ def test_vlasov_evolve_matches_oracle(sgdg, O, W, D, k, n, steps):
     assert np.array_equal(states[0], f0)
     ref = O.vlasov_rk4(D, k, n, oracle_ops(O, D, k, n), F, f0, dt, steps)
     assert rel(states[-1], ref) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,k,n,steps", [(1, 2, 4, 20), (2, 2, 3, 20), (1, 3, 4, 15), (1, 5, 3, 10)])
+def test_vlasov_matfree_matches_oracle(sgdg, O, W, D, k, n, steps):
+    F, f0 = W.vlasov_case(sgdg, D, k, n, seed=9)
+    dt = 2e-3
+    _, st = sgdg.vlasov_evolve(D, k, n, F, f0, 0.0, steps * dt, nsteps=steps, method="matfree")
+    ref = O.vlasov_rk4(D, k, n, oracle_ops(O, D, k, n), F, f0, dt, steps)
+    assert rel(st[-1], ref) < 1e-6
+    _, sp = sgdg.vlasov_evolve(D, k, n, F, f0, 0.0, steps * dt, nsteps=steps, method="plain")
+    assert rel(st[-1], sp[-1]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_vlasov_in_a_mixed_batch_equals_alone(sgdg, W):
+    F1, f1 = W.vlasov_case(sgdg, 1, 2, 4, seed=1)
+    F2, f2 = W.vlasov_case(sgdg, 2, 2, 3, seed=2)
+    a0 = np.zeros(sgdg.get_size(2, 2, 4))
+    a0[:10] = 0.3
+    b = sgdg.Batch()
+    i1 = b.add_vlasov(1, 2, 4, f1, F1, 1e-3)
+    i2 = b.add_vlasov(2, 2, 3, f2, F2, 1e-3)
+    i3 = b.add("advect", 2, 2, 4, a0, 1e-3, a=[0.4, -0.2])
+    b.step(6)
+    for i, (Dx, k, n, f, F) in [(i1, (1, 2, 4, f1, F1)), (i2, (2, 2, 3, f2, F2))]:
+        alone = sgdg.Batch()
+        j = alone.add_vlasov(Dx, k, n, f, F, 1e-3)
+        alone.step(6)
+        assert np.array_equal(b.state(i), alone.state(j))
+    alone = sgdg.Batch()
+    j = alone.add("advect", 2, 2, 4, a0, 1e-3, a=[0.4, -0.2])
+    alone.step(6)
+    assert np.array_equal(b.state(i3), alone.state(j))
