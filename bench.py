@@ -232,11 +232,14 @@ def uneven_batch_leg(sg, stream, steps=50, warmup=5):
             "shapes_wlog_coop": shapes}
 
 
-def vlasov_leg(sg, steps):
+def vlasov_leg(sg, stream, steps, batch=16):
     """Vlasov-type transport in 2x2v phase space (D = 2 space dimensions),
     sparse k=2, n=8: seeded force E(x) of amplitude 0.1, Maxwellian in v
-    (sigma 0.15) times (1 + 0.05 cos 2 pi x_1); FP64 sparse operators on the
-    GPU (derivatives, nodal transforms, point products), RK4."""
+    (sigma 0.15) times (1 + 0.05 cos 2 pi x_1), RK4.  Two forms: FP64 sparse
+    operators on the GPU (derivatives, nodal transforms, point products), and
+    the matrix-free FP32 form (pencil sweeps of the transforms, FP64 RK state)
+    for one solve and for a batch of independent solves in one launch per
+    stage; the two forms' results after the same steps are compared."""
     import importlib
     W = importlib.import_module(sg.__name__ + ".workloads")
     sv = importlib.import_module(sg.__name__ + ".serving")
@@ -258,11 +261,40 @@ def vlasov_leg(sg, steps):
     nnz = {"%s_to_%s" % w: int(op.transform(*w).nnz)
            for w in [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"), ("nodal", "modal")]}
     op.close()
-    return {"workload": "Vlasov 2x2v (D=4 phase space), sparse k=2, n=8, RK4", "state_dofs": int(f0.size),
-            "steps": steps, "dt": dt, "form": "FP64 sparse operators (CSR SpMV), graph per RK4 step",
-            "value": f0.size * 4.0 / per_step, "unit": UNIT, "ms_per_step": 1e3 * per_step,
-            "wall_s_end_to_end": total, "host_setup_s": setup, "transform_nnz": nnz,
-            "rel_l2_change_of_f": float(np.linalg.norm(st[-1] - f0) / np.linalg.norm(f0))}
+    N = int(f0.size)
+    out = {"workload": "Vlasov 2x2v (D=4 phase space), sparse k=2, n=8, RK4", "state_dofs": N,
+           "steps": steps, "dt": dt, "unit": UNIT,
+           "plain_fp64": {"form": "FP64 sparse operators (CSR SpMV), graph per RK4 step",
+                          "value": N * 4.0 / per_step, "ms_per_step": 1e3 * per_step,
+                          "wall_s_end_to_end": total, "host_setup_s": setup, "transform_nnz": nnz},
+           "rel_l2_change_of_f": float(np.linalg.norm(st[-1] - f0) / np.linalg.norm(f0))}
+    # matrix-free, one solve: same steps, then the difference to the FP64 result
+    b = sg.Batch()
+    b.set_stream(stream.cuda_stream)
+    b.add_vlasov(Dx, k, n, f0, F, dt)
+    b.autotune()  # the tile shape of (4, 2) is kept for the batches below
+    b.close()
+    b = sg.Batch()
+    b.set_stream(stream.cuda_stream)
+    i = b.add_vlasov(Dx, k, n, f0, F, dt)
+    b.step(steps)
+    mf = b.state(i)
+    ms_one = timed_steps(b, stream, 20, 3)
+    b.close()
+    out["matfree_one"] = {"form": "FP32 pencil sweeps, FP64 RK state, graph per RK4 step",
+                          "value": N * 4.0 / (ms_one / 1e3), "ms_per_step": ms_one,
+                          "rel_l2_vs_plain_fp64": float(np.linalg.norm(mf - st[-1]) / np.linalg.norm(st[-1]))}
+    # matrix-free, a batch of independent solves (different seeded forces and data)
+    b = sg.Batch()
+    b.set_stream(stream.cuda_stream)
+    for s in range(batch):
+        Fs, fs = W.vlasov_case(sg, Dx, k, n, seed=100 + s)
+        b.add_vlasov(Dx, k, n, fs, Fs, dt)
+    b.autotune()
+    ms_b = timed_steps(b, stream, 20, 3)
+    b.close()
+    out["matfree_batch"] = {"solves": batch, "value": batch * N * 4.0 / (ms_b / 1e3), "ms_per_step": ms_b}
+    return out
 
 
 PLAIN_MEASURE_MAX_N = 1_100_000  # larger plain operators take minutes to assemble on the host
@@ -496,7 +528,7 @@ def run_ours(args):
     line["config"]["tile_shape_wlog_coop"] = list(tile[:2])
     line["uneven_batch"] = uneven_batch_leg(sg, stream)
     if args.vlasov_steps > 0:
-        line["vlasov"] = vlasov_leg(sg, args.vlasov_steps)
+        line["vlasov"] = vlasov_leg(sg, stream, args.vlasov_steps)
     if args.serve_requests > 0:
         line["serving"] = serving_leg(sg, args)
     if cpu:
