@@ -99,9 +99,23 @@ struct MFItem {
     int32_t kd1;       // pass: k^d
     int32_t kDm1;      // pass: k^(D-1)
     int32_t rlong;     // pass: leading row blocks swept by a whole warp each
+    uint32_t rmagic;   // pass: g / R = (g * rmagic) >> rshift for 0 <= g < 2^31 (mf_divisor)
+    int32_t rshift;
 };
 
+// (magic, shift) of the division by an invariant d >= 1 for numerators below
+// 2^31: Granlund and Montgomery (PLDI 1994), Theorem 4.2 with N = 31,
+// l = ceil(log2 d), magic = floor(2^(31+l) / d) + 1 (< 2^32), shift = 31 + l.
+inline void mf_divisor(int32_t d, uint32_t* magic, int32_t* shift) {
+    int l = 0;
+    while ((1LL << l) < (long long)d) l++;
+    *magic = (uint32_t)(((1ULL << (31 + l)) / (unsigned long long)d) + 1ULL);
+    *shift = 31 + l;
+}
+
 constexpr int kMFThreads = 256;  // 8 warps share one copy of the operator table
+constexpr int kMFThreadsLog2 = 8;
+static_assert(1 << kMFThreadsLog2 == kMFThreads, "kMFThreadsLog2");
 constexpr int kSpinLimit = 1 << 22;  // polls of a dependency counter before giving up
 
 // Tile shape of the pass tiles of one (D, k), chosen by the autotuner:
@@ -121,7 +135,12 @@ void mf_clear_tiles();
 
 inline int mf_rlong(int lmax, int coop) { return lmax > coop ? 1 << (lmax - 1 - coop) : 0; }
 // bytes of dynamic shared memory a pass tile of W columns over nrb row blocks needs
-inline size_t mf_tile_smem(int k, int nrb, int W) { return 4 * (3 * (size_t)W + (size_t)k * nrb * W * 2); }
+// (three int tables per column, an int2 per row padded to an even row count,
+// the tile and its sweep output)
+inline size_t mf_tile_smem(int k, int nrb, int W) {
+    const size_t m = (size_t)k * nrb;
+    return 4 * (3 * (size_t)W + 2 * ((m + 1) & ~(size_t)1) + m * W * 2);
+}
 constexpr size_t kMFTileSmemMax = 64 * 1024;  // wider tiles are narrowed to fit
 // columns of a pass tile (a power of two)
 inline int mf_tile_cols(int k, int cpt, int nrb, int wlog) {

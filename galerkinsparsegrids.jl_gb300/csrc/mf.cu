@@ -23,6 +23,7 @@
 #include <cstddef>
 
 #include "engine.h"
+#include "cvt.cuh"
 #include "rk.cuh"
 
 namespace sgdg {
@@ -46,21 +47,6 @@ __device__ __forceinline__ int ld_relaxed(const int* p) {
     int v;
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
     return v;
-}
-
-struct TileCols {  // per-column tables in shared memory
-    const int* slot;  // solve slot of the column (-1: padding)
-    const int* a;     // offset within the solve of the column's row-0 element, low part
-    const int* b;     // high cell part, shifted left by the row's level
-};
-
-template <int K>
-__device__ __forceinline__ int elem_off(const int* __restrict__ boff, const TileCols& cols, int kD, int lp, int kd1,
-                                        int rb, int i, int j) {
-    const int l = block_level(rb);
-    const int lc = l > 2 ? l - 2 : 0;
-    const int cd0 = l >= 2 ? rb - (1 << (l - 2)) : 0;
-    return boff[l - 1] + cols.a[j] + (cols.b[j] << lc) + kD * (cd0 << lp) + i * kd1;
 }
 
 // acc[i][c] += S(rb, cb)[i][jj] * src[cb*K + jj][jq*CPT + c] over the stored
@@ -177,10 +163,25 @@ __device__ __forceinline__ void wait_counter(const int* ctr, int need, int* err)
     }
 }
 
-// One pencil tile; sboff holds the pencil's level-block offsets.
+// Runs col(j, r0, rstep) for the columns j of a W-column tile: consecutive
+// threads take consecutive columns (min(W, kMFThreads) of them), and each
+// thread then walks its column's rows r0, r0 + rstep, ... (so per-column
+// values are computed once per thread and a warp's accesses follow a row).
+template <class ColFn>
+__device__ __forceinline__ void tile_columns(int W, int lw, ColFn&& col) {
+    const int cl = lw < kMFThreadsLog2 ? lw : kMFThreadsLog2;
+    const int r0 = (int)threadIdx.x >> cl, rstep = kMFThreads >> cl;
+    for (int j = (int)threadIdx.x & ((1 << cl) - 1); j < W; j += 1 << cl) col(j, r0, rstep);
+}
+
+// One pencil tile.  Element (row, j) of the tile lives at offset
+// rinfo[row].x + ca[j] + (cb[j] << rinfo[row].y) of solve cslot[j]: the
+// row part (level block, cell and mode along d) and the column part (cells
+// and modes of the other dimensions, the high cell part scaled by the row
+// level's cell count) are tabulated once per tile in shared memory.
 template <int K, int CPT, bool WAVE>
-__device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, const int* sboff, int stage,
-                          int in_sel, float* smem, const int* ctr, int* err) {
+__device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int stage, int in_sel, float* smem,
+                          const int* ctr, int* err) {
     const int tid = threadIdx.x;
     const int nrb = 1 << (it.lmax - 1);
     const int m = nrb * K;
@@ -189,16 +190,17 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     int* cslot = reinterpret_cast<int*>(smem);
     int* ca = cslot + W;
     int* cb = ca + W;
-    float* X = reinterpret_cast<float*>(cb + W);  // 12W bytes in: 16-aligned for W % 4 == 0, 8 for W % 2 == 0
+    int2* rinfo = reinterpret_cast<int2*>(cb + W);              // 12W bytes in: 8-aligned (W even)
+    float* X = reinterpret_cast<float*>(rinfo + ((m + 1) & ~1));  // + 8 mpad: 16-aligned for W % 4 == 0
     float* Y = X + m * W;
     const int kD = C.kD, kd1 = it.kd1, lp = it.lp, R = it.R, kDm1 = it.kDm1;
     for (int j = tid; j < W; j += kMFThreads) {
         if (j < Wv) {
             // column g of the class: slot, then (cells, modes) of the other dimensions
             const int g = it.g0 + j;
-            const int slot = g / R, r = g - slot * R;
-            const int cr = r / kDm1, mr = r - cr * kDm1;
-            const int mq = mr / kd1;
+            const int slot = div_invariant(g, it.rmagic, it.rshift), r = g - slot * R;
+            const int cr = div_pow<K>(r, C.D - 1), mr = r - cr * kDm1;
+            const int mq = div_pow<K>(mr, it.d);
             cslot[j] = slot;
             ca[j] = kD * (cr & ((1 << lp) - 1)) + (mr - mq * kd1) + mq * kd1 * K;
             cb[j] = kD * ((cr >> lp) << lp);
@@ -208,34 +210,51 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             cb[j] = 0;
         }
     }
+    for (int row = tid; row < m; row += kMFThreads) {
+        // row block rb of level l: cell cd0 of the level, mode i along d
+        const int rb = row / K, i = row - rb * K;
+        const int l = block_level(rb);
+        const int cd0 = l >= 2 ? rb - (1 << (l - 2)) : 0;
+        rinfo[row] = make_int2((int)C.blockoff[it.boff + l - 1] + kD * (cd0 << lp) + i * kd1, l > 2 ? l - 2 : 0);
+    }
     // an input written by the previous phase of this launch must be complete
     if ((it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
-    const TileCols cols{cslot, ca, cb};
     const float* __restrict__ uin = C.u[in_sel];
-    const int ne = m << lw;
     if (it.src < 0) {
         // gather the stage input (written by the previous launch) into X
-        for (int e = tid; e < ne; e += kMFThreads) {
-            const int row = e >> lw, j = e & (W - 1);
+        tile_columns(W, lw, [&](int j, int r0, int rstep) {
+            float* xc = X + j;
             const int s = cslot[j];
             if (s < 0) {
-                X[e] = 0.f;
-                continue;
+                for (int row = r0; row < m; row += rstep) xc[row * W] = 0.f;
+                return;
             }
-            const int rb = row / K, i = row - rb * K;
-            cp_async4(X + e, uin + (size_t)s * C.Ns + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j));
-        }
+            const float* base = uin + (size_t)s * C.Ns + ca[j];
+            const int bj = cb[j];
+            for (int row = r0; row < m; row += rstep) {
+                const int2 ri = rinfo[row];
+                cp_async4(xc + row * W, base + ri.x + (bj << ri.y));
+            }
+        });
         cp_async_wait_all();
     } else {
         // a scratch vector written in this launch by other SMs: L2 loads (.cg)
         const float* __restrict__ vin = C.vb[it.src];
-        for (int e = tid; e < ne; e += kMFThreads) {
-            const int row = e >> lw, j = e & (W - 1);
+        tile_columns(W, lw, [&](int j, int r0, int rstep) {
+            float* xc = X + j;
             const int s = cslot[j];
-            const int rb = row / K, i = row - rb * K;
-            X[e] = s < 0 ? 0.f : __ldcg(vin + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j));
-        }
+            if (s < 0) {
+                for (int row = r0; row < m; row += rstep) xc[row * W] = 0.f;
+                return;
+            }
+            const float* base = vin + (size_t)s * C.N + ca[j];
+            const int bj = cb[j];
+            for (int row = r0; row < m; row += rstep) {
+                const int2 ri = rinfo[row];
+                xc[row * W] = __ldcg(base + ri.x + (bj << ri.y));
+            }
+        });
     }
     __syncthreads();
     const int lwq = lw - (CPT == 4 ? 2 : 1);
@@ -268,36 +287,43 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         // product w_d .* result added into the point-basis accumulator
         float* __restrict__ out = C.vb[it.dst];
         const bool wacc = (it.flags & TILE_WACC) != 0;
-        for (int e = tid; e < ne; e += kMFThreads) {
-            const int row = e >> lw, j = e & (W - 1);
+        tile_columns(W, lw, [&](int j, int r0, int rstep) {
             const int s = cslot[j];
-            if (s < 0) continue;
-            const int rb = row / K, i = row - rb * K;
-            const int off = elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
-            float* op = out + (size_t)s * C.N + off;
-            float v = Z[e];
-            if (wacc) {
-                const float* wp = C.vw + (size_t)s * 2 * C.D * C.N + (size_t)it.wsel * C.N + off;
-                v = fmaf(__ldg(wp), v, __ldg(wp + (size_t)C.D * C.N) * v);
-                if (!first) v += __ldcg(op);
+            if (s < 0) return;
+            float* oc = out + (size_t)s * C.N + ca[j];
+            const float* wc = C.vw + (size_t)s * 2 * C.D * C.N + (size_t)it.wsel * C.N + ca[j];
+            const size_t wlo = (size_t)C.D * C.N;
+            const int bj = cb[j];
+            for (int row = r0; row < m; row += rstep) {
+                const int2 ri = rinfo[row];
+                const int off = ri.x + (bj << ri.y);
+                float v = Z[row * W + j];
+                if (wacc) {
+                    v = fmaf(__ldg(wc + off), v, __ldg(wc + wlo + off) * v);
+                    if (!first) v += __ldcg(oc + off);
+                }
+                __stcg(oc + off, v);
             }
-            __stcg(op, v);
-        }
+        });
         return;
     }
     if (!(it.flags & TILE_RK)) {
         // partial sum sum_{q <= d} coef_q D_q u of this tile's elements
-        for (int e = tid; e < ne; e += kMFThreads) {
-            const int row = e >> lw, j = e & (W - 1);
+        tile_columns(W, lw, [&](int j, int r0, int rstep) {
             const int s = cslot[j];
-            if (s < 0) continue;
-            const int rb = row / K, i = row - rb * K;
-            float* rp = C.rhs + (size_t)s * C.N + elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
-            const float z = Z[e];
-            float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
-            if (!first) v += __ldcg(rp);
-            __stcg(rp, v);
-        }
+            if (s < 0) return;
+            float* rc = C.rhs + (size_t)s * C.N + ca[j];
+            const float chi = __ldg(C.coef + s * 16 + it.d), clo = __ldg(C.coef + s * 16 + 8 + it.d);
+            const int bj = cb[j];
+            for (int row = r0; row < m; row += rstep) {
+                const int2 ri = rinfo[row];
+                float* rp = rc + ri.x + (bj << ri.y);
+                const float z = Z[row * W + j];
+                float v = fmaf(chi, z, clo * z);
+                if (!first) v += __ldcg(rp);
+                __stcg(rp, v);
+            }
+        });
         return;
     }
     // last dimension: the right-hand side of each element is complete here, so
@@ -306,43 +332,48 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     // pencils of one dimension partition the coefficients, so every state
     // element is updated once per stage.
     float* __restrict__ uout = C.u[in_sel ^ 1];
-    for (int e = tid; e < ne; e += kMFThreads) {
-        const int row = e >> lw, j = e & (W - 1);
+    tile_columns(W, lw, [&](int j, int r0, int rstep) {
         const int s = cslot[j];
-        if (s < 0 || __ldg(C.status + s) != 0) continue;
-        const int rb = row / K, i = row - rb * K;
-        const int off = elem_off<K>(sboff, cols, kD, lp, kd1, rb, i, j);
-        const size_t b = (size_t)s * C.Ns;
-        const size_t iv = b + (WAVE ? (size_t)C.N : 0) + off;  // the component D acts on
-        // issue every load of the element before the arithmetic
-        const float z = Z[e];
-        const float prev = first ? 0.f : __ldcg(C.rhs + (size_t)s * C.N + off);
-        double yv = __ldcg(C.y + iv), av = stage != 1 ? __ldcg(C.acc + iv) : 0.0;
-        double yf = 0.0, af = 0.0, kf = 0.0;
-        if (WAVE) {
-            yf = __ldcg(C.y + b + off);
-            af = stage != 1 ? __ldcg(C.acc + b + off) : 0.0;
-            kf = (double)__ldcg(uin + b + C.N + off);
-        }
-        float v = fmaf(__ldg(C.coef + s * 16 + it.d), z, __ldg(C.coef + s * 16 + 8 + it.d) * z);
-        if (!first) v += prev;
+        if (s < 0 || __ldg(C.status + s) != 0) return;
+        const size_t b = (size_t)s * C.Ns + ca[j];         // the column's f component (wave) or state
+        const size_t bv = b + (WAVE ? (size_t)C.N : 0);    // the component D acts on
+        const float* rc = C.rhs + (size_t)s * C.N + ca[j];
+        const float chi = __ldg(C.coef + s * 16 + it.d), clo = __ldg(C.coef + s * 16 + 8 + it.d);
         const double dt = __ldg(C.dt + 3 * s), hdt = __ldg(C.dt + 3 * s + 1), dt6 = __ldg(C.dt + 3 * s + 2);
-        double un;
-        rk_stage(stage, dt, hdt, dt6, (double)v, yv, av, un);
-        if (stage == 4)
-            __stcg(C.y + iv, yv);
-        else
-            __stcg(C.acc + iv, av);
-        __stcg(uout + iv, (float)un);
-        if (WAVE) {
-            rk_stage(stage, dt, hdt, dt6, kf, yf, af, un);
+        const int bj = cb[j];
+        for (int row = r0; row < m; row += rstep) {
+            const int2 ri = rinfo[row];
+            const int off = ri.x + (bj << ri.y);
+            // issue every load of the element before the arithmetic
+            const float z = Z[row * W + j];
+            const float prev = first ? 0.f : __ldcg(rc + off);
+            double yv = __ldcg(C.y + bv + off), av = stage != 1 ? __ldcg(C.acc + bv + off) : 0.0;
+            double yf = 0.0, af = 0.0;
+            float kf = 0.f;
+            if (WAVE) {
+                yf = __ldcg(C.y + b + off);
+                af = stage != 1 ? __ldcg(C.acc + b + off) : 0.0;
+                kf = __ldcg(uin + b + C.N + off);
+            }
+            float v = fmaf(chi, z, clo * z);
+            if (!first) v += prev;
+            double un;
+            rk_stage(stage, dt, hdt, dt6, f32_to_f64(v), yv, av, un);
             if (stage == 4)
-                __stcg(C.y + b + off, yf);
+                __stcg(C.y + bv + off, yv);
             else
-                __stcg(C.acc + b + off, af);
-            __stcg(uout + b + off, (float)un);
+                __stcg(C.acc + bv + off, av);
+            __stcg(uout + bv + off, f64_to_f32(un));
+            if (WAVE) {
+                rk_stage(stage, dt, hdt, dt6, f32_to_f64(kf), yf, af, un);
+                if (stage == 4)
+                    __stcg(C.y + b + off, yf);
+                else
+                    __stcg(C.acc + b + off, af);
+                __stcg(uout + b + off, f64_to_f32(un));
+            }
         }
-    }
+    });
 }
 
 __global__ void __launch_bounds__(kMFThreads, 3)
@@ -356,7 +387,6 @@ __global__ void __launch_bounds__(kMFThreads, 3)
     __shared__ MFClass s_cls;
     __shared__ int s_cls_id;   // class in s_cls (-1: none)
     __shared__ int s_cached;   // class whose table is in shared memory (-1: none)
-    __shared__ int s_off[32];  // level-block offsets of the item's pencil (N < 2^31)
     const int tid = threadIdx.x;
     constexpr int kItemWords = sizeof(MFItem) / 4;
     constexpr int kClsWords = sizeof(MFClass) / 4;
@@ -387,7 +417,6 @@ __global__ void __launch_bounds__(kMFThreads, 3)
         const MFItem& it = s_it;
         const MFClass& C = s_cls;
         if (tid == 0) s_cls_id = it.cls;  // read again only after the next barrier
-        if (tid < it.lmax) s_off[tid] = (int)C.blockoff[it.boff + tid];  // seen after pass_tile's first barrier
         OpTable T{C.s_rowptr, C.s_ent, C.s_val};
         if (it.tab != TABLE_DERIVATIVE) {  // a nodal transform: read through L1
             T = OpTable{C.t_rowptr[it.tab], C.t_ent[it.tab], C.t_val[it.tab]};
@@ -406,16 +435,16 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             T = OpTable{trow, tent, tval};
         }
         switch (C.k * 2 + (C.kind == MF_KIND_WAVE ? 1 : 0)) {  // Vlasov sweeps once, like advection
-            case 2: pass_tile<1, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 3: pass_tile<1, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 4: pass_tile<2, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 5: pass_tile<2, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 6: pass_tile<3, 4, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 7: pass_tile<3, 4, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 8: pass_tile<4, 2, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 9: pass_tile<4, 2, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 10: pass_tile<5, 2, false>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
-            case 11: pass_tile<5, 2, true>(it, C, T, s_off, stage, in_sel, tile, ctr, err); break;
+            case 2: pass_tile<1, 4, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 3: pass_tile<1, 4, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 4: pass_tile<2, 4, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 5: pass_tile<2, 4, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 6: pass_tile<3, 4, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 7: pass_tile<3, 4, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 8: pass_tile<4, 2, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 9: pass_tile<4, 2, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 10: pass_tile<5, 2, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
+            case 11: pass_tile<5, 2, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
             default: break;
         }
         __syncthreads();

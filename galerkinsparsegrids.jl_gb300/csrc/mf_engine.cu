@@ -426,6 +426,7 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                         it.lp = p.lp;
                         it.boff = c.boff_index[bi + pi];
                         it.R = (int32_t)p.R;
+                        mf_divisor(it.R, &it.rmagic, &it.rshift);
                         it.g0 = (int32_t)g0;
                         it.W = Wp;
                         it.Wv = (int32_t)std::min<int64_t>(Wp, cend - g0);

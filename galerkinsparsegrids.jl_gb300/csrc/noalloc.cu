@@ -155,6 +155,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
                     it.lp = p.lp;
                     it.boff = pb;
                     it.R = (int32_t)p.R;
+                    mf_divisor(it.R, &it.rmagic, &it.rshift);
                     it.g0 = (int32_t)g0;
                     it.W = Wp;
                     it.Wv = (int32_t)std::min<int64_t>(Wp, p.R - g0);
