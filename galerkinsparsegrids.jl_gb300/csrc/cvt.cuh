@@ -10,17 +10,24 @@
 //               even on the 29 dropped bits; a carry out of the mantissa
 //               increments the exponent (and reaches infinity exactly when
 //               round-to-nearest overflows).
-// Zero, subnormal, infinite and NaN inputs, and f64 values outside the
-// normal binary32 range, take the hardware conversion (a rarely taken branch).
+// Signed zeros are handled inline; subnormal, infinite and NaN inputs, and
+// f64 values outside the normal binary32 range, take the hardware conversion.
 #pragma once
 
 namespace sgdg {
 
+// The rare inputs go through real calls: a call is not if-converted, so the
+// hardware conversion (an FP64-pipe instruction) is not issued, predicated
+// off, for every element.
+__device__ __noinline__ double f32_to_f64_rare(float f) { return (double)f; }
+__device__ __noinline__ float f64_to_f32_rare(double x) { return (float)x; }
+
 __device__ __forceinline__ double f32_to_f64(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
-    if (e - 1u >= 254u) return (double)f;  // zero, subnormal, inf, nan
-    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0x000fffffu);
+    if (e - 1u >= 254u && (u << 1) != 0u) return f32_to_f64_rare(f);  // subnormal, inf, nan
+    // normal, or a signed zero (e == 0, mantissa 0)
+    const unsigned hi = (u & 0x80000000u) | (e != 0u ? ((e + 896u) << 20) | ((u >> 3) & 0x000fffffu) : 0u);
     return __hiloint2double((int)hi, (int)(u << 29));
 }
 
@@ -28,7 +35,10 @@ __device__ __forceinline__ float f64_to_f32(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
     const unsigned e = (hi >> 20) & 0x7ffu;
-    if (e - 897u >= 254u) return (float)x;  // |x| < 2^-126, |x| >= 2^128, inf, nan
+    if (e - 897u >= 254u) {                                // |x| < 2^-126, |x| >= 2^128, inf, nan
+        if (((hi << 1) | lo) == 0u) return __uint_as_float(hi);  // a signed zero
+        return f64_to_f32_rare(x);
+    }
     unsigned r = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
     const unsigned rest = lo & 0x1fffffffu;  // the dropped bits; half an ulp is 2^28
     r += (rest > 0x10000000u ? 1u : 0u) | (rest == 0x10000000u ? (r & 1u) : 0u);

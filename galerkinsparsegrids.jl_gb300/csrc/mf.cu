@@ -37,6 +37,7 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+
 __device__ __forceinline__ int ld_acquire(const int* p) {
     int v;
     asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
@@ -179,6 +180,8 @@ __device__ __forceinline__ void tile_columns(int W, int lw, ColFn&& col) {
 // row part (level block, cell and mode along d) and the column part (cells
 // and modes of the other dimensions, the high cell part scaled by the row
 // level's cell count) are tabulated once per tile in shared memory.
+constexpr int kOutRows = 4;       // rows per batch of the output loops
+
 template <int K, int CPT, bool WAVE>
 __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int stage, int in_sel, float* smem,
                           const int* ctr, int* err) {
@@ -282,6 +285,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     if (!(it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
     const bool first = (it.flags & TILE_FIRST) != 0;
+    // The output loops take kOutRows rows of a column at a time and issue all
+    // their loads before any store: a store may alias a later row's load as far
+    // as the compiler can tell, so a row-at-a-time loop is one global round
+    // trip per row.  Rows past the end load a copy of the last row (in bounds)
+    // and store nothing.
     if (it.flags & (TILE_STORE | TILE_WACC)) {
         // Vlasov: a transform's result to a scratch vector, or the point
         // product w_d .* result added into the point-basis accumulator
@@ -294,15 +302,29 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const float* wc = C.vw + (size_t)s * 2 * C.D * C.N + (size_t)it.wsel * C.N + ca[j];
             const size_t wlo = (size_t)C.D * C.N;
             const int bj = cb[j];
-            for (int row = r0; row < m; row += rstep) {
-                const int2 ri = rinfo[row];
-                const int off = ri.x + (bj << ri.y);
-                float v = Z[row * W + j];
-                if (wacc) {
-                    v = fmaf(__ldg(wc + off), v, __ldg(wc + wlo + off) * v);
-                    if (!first) v += __ldcg(oc + off);
+            for (int row0 = r0; row0 < m; row0 += kOutRows * rstep) {
+                int off[kOutRows];
+                float v[kOutRows], wh[kOutRows], wl[kOutRows], prev[kOutRows];
+#pragma unroll
+                for (int u = 0; u < kOutRows; u++) {
+                    const int row = min(row0 + u * rstep, m - 1);
+                    const int2 ri = rinfo[row];
+                    off[u] = ri.x + (bj << ri.y);
+                    v[u] = Z[row * W + j];
+                    wh[u] = wacc ? __ldg(wc + off[u]) : 0.f;
+                    wl[u] = wacc ? __ldg(wc + wlo + off[u]) : 0.f;
+                    prev[u] = wacc && !first ? __ldcg(oc + off[u]) : 0.f;
                 }
-                __stcg(oc + off, v);
+#pragma unroll
+                for (int u = 0; u < kOutRows; u++) {
+                    if (row0 + u * rstep >= m) break;
+                    float x = v[u];
+                    if (wacc) {
+                        x = fmaf(wh[u], x, wl[u] * x);
+                        if (!first) x += prev[u];
+                    }
+                    __stcg(oc + off[u], x);
+                }
             }
         });
         return;
@@ -315,13 +337,24 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             float* rc = C.rhs + (size_t)s * C.N + ca[j];
             const float chi = __ldg(C.coef + s * 16 + it.d), clo = __ldg(C.coef + s * 16 + 8 + it.d);
             const int bj = cb[j];
-            for (int row = r0; row < m; row += rstep) {
-                const int2 ri = rinfo[row];
-                float* rp = rc + ri.x + (bj << ri.y);
-                const float z = Z[row * W + j];
-                float v = fmaf(chi, z, clo * z);
-                if (!first) v += __ldcg(rp);
-                __stcg(rp, v);
+            for (int row0 = r0; row0 < m; row0 += kOutRows * rstep) {
+                int off[kOutRows];
+                float z[kOutRows], prev[kOutRows];
+#pragma unroll
+                for (int u = 0; u < kOutRows; u++) {
+                    const int row = min(row0 + u * rstep, m - 1);
+                    const int2 ri = rinfo[row];
+                    off[u] = ri.x + (bj << ri.y);
+                    z[u] = Z[row * W + j];
+                    prev[u] = first ? 0.f : __ldcg(rc + off[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < kOutRows; u++) {
+                    if (row0 + u * rstep >= m) break;
+                    float v = fmaf(chi, z[u], clo * z[u]);
+                    if (!first) v += prev[u];
+                    __stcg(rc + off[u], v);
+                }
             }
         });
         return;
@@ -332,6 +365,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     // pencils of one dimension partition the coefficients, so every state
     // element is updated once per stage.
     float* __restrict__ uout = C.u[in_sel ^ 1];
+    constexpr int R_ = WAVE ? 2 : kOutRows;  // the wave carries two components per row
     tile_columns(W, lw, [&](int j, int r0, int rstep) {
         const int s = cslot[j];
         if (s < 0 || __ldg(C.status + s) != 0) return;
@@ -341,36 +375,49 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         const float chi = __ldg(C.coef + s * 16 + it.d), clo = __ldg(C.coef + s * 16 + 8 + it.d);
         const double dt = __ldg(C.dt + 3 * s), hdt = __ldg(C.dt + 3 * s + 1), dt6 = __ldg(C.dt + 3 * s + 2);
         const int bj = cb[j];
-        for (int row = r0; row < m; row += rstep) {
-            const int2 ri = rinfo[row];
-            const int off = ri.x + (bj << ri.y);
-            // issue every load of the element before the arithmetic
-            const float z = Z[row * W + j];
-            const float prev = first ? 0.f : __ldcg(rc + off);
-            double yv = __ldcg(C.y + bv + off), av = stage != 1 ? __ldcg(C.acc + bv + off) : 0.0;
-            double yf = 0.0, af = 0.0;
-            float kf = 0.f;
-            if (WAVE) {
-                yf = __ldcg(C.y + b + off);
-                af = stage != 1 ? __ldcg(C.acc + b + off) : 0.0;
-                kf = __ldcg(uin + b + C.N + off);
+        for (int row0 = r0; row0 < m; row0 += R_ * rstep) {
+            int off[R_];
+            float z[R_], prev[R_], kf[R_];
+            double yv[R_], av[R_], yf[R_], af[R_];
+#pragma unroll
+            for (int u = 0; u < R_; u++) {
+                const int row = min(row0 + u * rstep, m - 1);
+                const int2 ri = rinfo[row];
+                off[u] = ri.x + (bj << ri.y);
+                z[u] = Z[row * W + j];
             }
-            float v = fmaf(chi, z, clo * z);
-            if (!first) v += prev;
-            double un;
-            rk_stage(stage, dt, hdt, dt6, f32_to_f64(v), yv, av, un);
-            if (stage == 4)
-                __stcg(C.y + bv + off, yv);
-            else
-                __stcg(C.acc + bv + off, av);
-            __stcg(uout + bv + off, f64_to_f32(un));
-            if (WAVE) {
-                rk_stage(stage, dt, hdt, dt6, f32_to_f64(kf), yf, af, un);
+#pragma unroll
+            for (int u = 0; u < R_; u++) {
+                prev[u] = first ? 0.f : __ldcg(rc + off[u]);
+                yv[u] = __ldcg(C.y + bv + off[u]);
+                av[u] = stage != 1 ? __ldcg(C.acc + bv + off[u]) : 0.0;
+                if (WAVE) {
+                    yf[u] = __ldcg(C.y + b + off[u]);
+                    af[u] = stage != 1 ? __ldcg(C.acc + b + off[u]) : 0.0;
+                    kf[u] = __ldcg(uin + b + C.N + off[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < R_; u++) {
+                if (row0 + u * rstep >= m) break;
+                const int o = off[u];
+                float v = fmaf(chi, z[u], clo * z[u]);
+                if (!first) v += prev[u];
+                double un;
+                rk_stage(stage, dt, hdt, dt6, f32_to_f64(v), yv[u], av[u], un);
                 if (stage == 4)
-                    __stcg(C.y + b + off, yf);
+                    __stcg(C.y + bv + o, yv[u]);
                 else
-                    __stcg(C.acc + b + off, af);
-                __stcg(uout + b + off, f64_to_f32(un));
+                    __stcg(C.acc + bv + o, av[u]);
+                __stcg(uout + bv + o, f64_to_f32(un));
+                if (WAVE) {
+                    rk_stage(stage, dt, hdt, dt6, f32_to_f64(kf[u]), yf[u], af[u], un);
+                    if (stage == 4)
+                        __stcg(C.y + b + o, yf[u]);
+                    else
+                        __stcg(C.acc + b + o, af[u]);
+                    __stcg(uout + b + o, f64_to_f32(un));
+                }
             }
         }
     });

@@ -23,7 +23,8 @@ int mf_columns_per_thread(int k);
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
 
-static constexpr int64_t kGroupReuseBytes = 6LL << 20;  // reused u + rhs per group (~4 groups in flight)
+static constexpr size_t kWaveLag = 2;       // steps between a group's consecutive phases in the work list
+constexpr int64_t kGroupReuseBytes = 6LL << 20;  // reused u + rhs per group (~4 groups in flight)
 
 // The arenas' cudaFree calls wait for outstanding work; the stream is not
 // touched here because a caller's stream may already be gone.
@@ -483,11 +484,16 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
     std::vector<std::vector<int>> ctr_of(groups.size());
     for (size_t g = 0; g < groups.size(); g++)
         for (size_t p = 0; p < groups[g].phases.size(); p++) ctr_of[g].push_back(nctr++);
+    // wavefront order: phase p of group g in step g + kWaveLag p, older groups
+    // first within a step, so a phase's predecessor was handed out kWaveLag
+    // steps earlier (about kWaveLag x phases-per-step items before it)
     size_t pmax = 0;
     for (auto& g : groups) pmax = std::max(pmax, g.phases.size());
-    for (size_t t = 0; t < groups.size() + pmax; t++)
-        for (size_t g = (t >= pmax ? t - pmax + 1 : 0); g <= t && g < groups.size(); g++) {
-            const size_t p = t - g;
+    const size_t G = groups.size();
+    for (size_t t = 0; t < G + kWaveLag * pmax; t++)
+        for (size_t pp = pmax; pp-- > 0;) {
+            if (t < kWaveLag * pp || t - kWaveLag * pp >= G) continue;
+            const size_t g = t - kWaveLag * pp, p = pp;
             if (p >= groups[g].phases.size()) continue;
             for (MFItem it : groups[g].phases[p]) {
                 it.done_ctr = ctr_of[g][p];
