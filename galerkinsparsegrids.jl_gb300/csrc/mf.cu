@@ -15,9 +15,13 @@
 // of the next stage (for the wave also the displacement field, whose
 // derivative is the velocity's stage input).
 //
-// Ordering: items are handed out in list order by an atomic counter; an item of phase p waits (bounded spin) until every item of
-// phase p-1 of its group has finished, so progress never depends on a later
-// item.  A wait that runs out sets *err and skips the item.
+// Ordering: items are handed out in list order by an atomic counter.  A CTA
+// claims its next item when the current one has passed all of its waits (at
+// the start of its output, so the claim's round trip overlaps the output),
+// and starts it right after that output.  An item of phase p waits (bounded
+// spin) until every item of phase p-1 of its group has finished; those come
+// earlier in the list, so progress never depends on a later item.  A wait
+// that runs out sets *err and the item goes on with what it has.
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -184,7 +188,7 @@ constexpr int kOutRows = 4;       // rows per batch of the output loops
 
 template <int K, int CPT, bool WAVE>
 __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int stage, int in_sel, float* smem,
-                          const int* ctr, int* err) {
+                          int* ctr, int* err, int* claim) {
     const int tid = threadIdx.x;
     const int nrb = 1 << (it.lmax - 1);
     const int m = nrb * K;
@@ -284,6 +288,10 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     // the partial sums of this group's previous pass must be complete
     if (!(it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
+    // claim the CTA's next item now (after every wait of this one): the
+    // atomic's round trip overlaps the output
+    int nxt = 0;
+    if (tid == 32) nxt = atomicAdd(ctr, 1);
     const bool first = (it.flags & TILE_FIRST) != 0;
     // The output loops take kOutRows rows of a column at a time and issue all
     // their loads before any store: a store may alias a later row's load as far
@@ -327,9 +335,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
                 }
             }
         });
-        return;
-    }
-    if (!(it.flags & TILE_RK)) {
+    } else if (!(it.flags & TILE_RK)) {
         // partial sum sum_{q <= d} coef_q D_q u of this tile's elements
         tile_columns(W, lw, [&](int j, int r0, int rstep) {
             const int s = cslot[j];
@@ -357,8 +363,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
                 }
             }
         });
-        return;
-    }
+    } else {
     // last dimension: the right-hand side of each element is complete here, so
     // the RK4 stage update of its state runs in place (for the wave also the
     // element's f component, whose derivative is the stage input of v).  The
@@ -421,6 +426,8 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             }
         }
     });
+    }
+    if (tid == 32) *claim = nxt;
 }
 
 __global__ void __launch_bounds__(kMFThreads, 3)
@@ -439,31 +446,40 @@ __global__ void __launch_bounds__(kMFThreads, 3)
     constexpr int kClsWords = sizeof(MFClass) / 4;
     static_assert(kItemWords <= 32, "item fits one warp");
     if (tid == 0) s_cls_id = s_cached = -1;
+    if (tid == 32) s_item = atomicAdd(ctr, 1);
+    int done = -1;  // thread 0: completion counter of the last finished item
     for (;;) {
-        // warp 0 takes the next item and stages it (and its class descriptor
-        // when the class changes)
-        if (tid < 32) {
-            int ii = 0;
-            if (tid == 0) ii = atomicAdd(ctr, 1);
-            ii = __shfl_sync(0xffffffffu, ii, 0);
+        __syncthreads();  // every thread has finished the previous item; s_item is claimed
+        // warp 1 stages the claimed item (and its class descriptor when the
+        // class changes) while thread 0 publishes the previous item's completion
+        if (tid >= 32 && tid < 64) {
+            const int lane = tid - 32;
+            const int ii = s_item;
             if (ii < nitems) {
                 int word = 0;
-                if (tid < kItemWords) {
-                    word = reinterpret_cast<const int*>(items + ii)[tid];
-                    reinterpret_cast<int*>(&s_it)[tid] = word;
+                if (lane < kItemWords) {
+                    word = reinterpret_cast<const int*>(items + ii)[lane];
+                    reinterpret_cast<int*>(&s_it)[lane] = word;
                 }
                 const int cls = __shfl_sync(0xffffffffu, word, 0) >> 16;  // MFItem::cls (second int16)
                 if (cls != s_cls_id)
-                    for (int w = tid; w < kClsWords; w += 32)
+                    for (int w = lane; w < kClsWords; w += 32)
                         reinterpret_cast<int*>(&s_cls)[w] = reinterpret_cast<const int*>(classes + cls)[w];
             }
-            if (tid == 0) s_item = ii;
+        }
+        if (tid == 0 && done >= 0) {
+            __threadfence();
+            atomicAdd(ctr + done, 1);
+            done = -1;
         }
         __syncthreads();
         if (s_item >= nitems) break;
         const MFItem& it = s_it;
         const MFClass& C = s_cls;
-        if (tid == 0) s_cls_id = it.cls;  // read again only after the next barrier
+        if (tid == 0) {
+            s_cls_id = it.cls;  // read again only after the next barrier
+            done = it.done_ctr;
+        }
         OpTable T{C.s_rowptr, C.s_ent, C.s_val};
         if (it.tab != TABLE_DERIVATIVE) {  // a nodal transform: read through L1
             T = OpTable{C.t_rowptr[it.tab], C.t_ent[it.tab], C.t_val[it.tab]};
@@ -482,22 +498,19 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             T = OpTable{trow, tent, tval};
         }
         switch (C.k * 2 + (C.kind == MF_KIND_WAVE ? 1 : 0)) {  // Vlasov sweeps once, like advection
-            case 2: pass_tile<1, 4, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 3: pass_tile<1, 4, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 4: pass_tile<2, 4, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 5: pass_tile<2, 4, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 6: pass_tile<3, 4, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 7: pass_tile<3, 4, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 8: pass_tile<4, 2, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 9: pass_tile<4, 2, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 10: pass_tile<5, 2, false>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            case 11: pass_tile<5, 2, true>(it, C, T, stage, in_sel, tile, ctr, err); break;
-            default: break;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            atomicAdd(ctr + it.done_ctr, 1);
+            case 2: pass_tile<1, 4, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 3: pass_tile<1, 4, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 4: pass_tile<2, 4, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 5: pass_tile<2, 4, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 6: pass_tile<3, 4, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 7: pass_tile<3, 4, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 8: pass_tile<4, 2, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 9: pass_tile<4, 2, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 10: pass_tile<5, 2, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 11: pass_tile<5, 2, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            default:
+                if (tid == 32) s_item = nitems;  // unreachable (k in 1..5): stop
+                break;
         }
     }
 }

@@ -23,7 +23,7 @@ int mf_columns_per_thread(int k);
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t st);
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
 
-static constexpr size_t kWaveLag = 2;       // steps between a group's consecutive phases in the work list
+static constexpr size_t kWaveLag = 3;       // steps between a group's consecutive phases in the work list
 constexpr int64_t kGroupReuseBytes = 6LL << 20;  // reused u + rhs per group (~4 groups in flight)
 
 // The arenas' cudaFree calls wait for outstanding work; the stream is not
