@@ -509,6 +509,82 @@ def vlasov_evolve(D, k, n, F_point, f0_modal, time0, time1, nout=2, order="rk4",
     return times, list(states)
 
 
+# ------------------------------------------------------------ evaluation ----
+def reconstruct_DG(D, k, n, coeffs, xs, scheme="sparse"):
+    """Value of the expansion with coefficient vector ``coeffs`` (the
+    reference's vector layout) at ``xs``: reconstruct_DG
+    (src/dg_methods.jl:150-165), batched and in FP64 on the GPU.  ``xs`` of
+    D coordinates gives a float; an (npts, D) array gives npts values.  A
+    coordinate below 0 or NaN raises SGDGError (code SGDG_EINVAL)."""
+    c = np.ascontiguousarray(coeffs, np.float64)
+    N = get_size(D, k, n, scheme)
+    if c.shape != (N,):
+        raise ValueError("coeffs must have %d entries" % N)
+    x = np.asarray(xs, np.float64)
+    single = x.ndim == 1
+    if x.shape[-1] != D or x.ndim > 2:
+        raise ValueError("xs must have D = %d coordinates per point" % D)
+    x = np.ascontiguousarray(x.reshape(-1, D))
+    out = np.empty(x.shape[0])
+    check(lib().sgdg_evaluate(D, k, n, _scheme(scheme), c, x.shape[0], x.reshape(-1), out))
+    return float(out[0]) if single else out
+
+
+class DGFunction:
+    """A coefficient vector as a function of points, evaluated on the GPU:
+    ``f(x)`` for x of D coordinates, or an (npts, D) array of points."""
+
+    def __init__(self, D, k, n, coeffs, scheme="sparse"):
+        self.D, self.k, self.n, self.scheme = D, k, n, scheme
+        self.coeffs = np.ascontiguousarray(coeffs, np.float64)
+
+    def __call__(self, xs):
+        return reconstruct_DG(self.D, self.k, self.n, self.coeffs, xs, self.scheme)
+
+
+def _values(f, pts):
+    """f at every row of pts: one vectorised call when f takes an (npts, D)
+    array (a DGFunction or a numpy expression), else one call per point
+    with the point as a tuple, as the reference's functions take it."""
+    try:
+        v = np.asarray(f(pts), np.float64)
+        if v.shape == (pts.shape[0],):
+            return v
+    except Exception:
+        pass
+    return np.array([float(f(tuple(p))) for p in pts])
+
+
+def monte_carlo(f, D, count=1000, rng=None):
+    """Mean of f over ``count`` uniform points of [0, 1]^D (src/error_measure.jl:12-19)."""
+    rng = rng if rng is not None else np.random.default_rng()
+    return float(np.mean(_values(f, rng.random((count, D)))))
+
+
+def mcerr(f, g, D, count=1000, rng=None):
+    """Root-mean-square of f - g over ``count`` uniform points of [0, 1]^D
+    (src/error_measure.jl:39-41); f or g may be a DGFunction (GPU)."""
+    rng = rng if rng is not None else np.random.default_rng()
+    pts = rng.random((count, D))
+    return float(np.sqrt(np.mean((_values(f, pts) - _values(g, pts)) ** 2)))
+
+
+def mcerr2(f, g, D, batch=50, Z=1.0, rng=None):
+    """mcerr with the adaptive batching of monte_carlo2
+    (src/error_measure.jl:21-37, 43-45): batches of ``batch`` points until a
+    new batch's mean is within Z standard deviations of the earlier batch
+    means."""
+    rng = rng if rng is not None else np.random.default_rng()
+    means = []
+    while True:
+        pts = rng.random((batch, D))
+        sq = (_values(f, pts) - _values(g, pts)) ** 2
+        if len(means) > 1 and abs(np.mean(sq) - np.mean(means)) / np.std(means, ddof=1) < Z:
+            break
+        means.append(float(np.mean(sq)))
+    return float(np.sqrt(np.mean(means)))
+
+
 # --------------------------------------------------------------- batches ----
 class Batch:
     """Independent solves of uneven (D, k, n) advanced together by the

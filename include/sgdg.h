@@ -248,6 +248,19 @@ int sgdg_server_cancel(sgdg_server *s, int64_t request_id);
  * DOF-updates (state coefficients x RK stages) executed so far. */
 int sgdg_server_counts(sgdg_server *s, int64_t *queued, int64_t *running, int64_t *finished, double *dof_updates);
 
+/* ---------------------------------------------------------- evaluation --
+ * Point values of a coefficient vector (the reference's vector layout) at
+ * npts points xs[p * D + d] in [0, 1]^D: reconstruct_DG
+ * (src/dg_methods.jl:150-165) batched, in FP64 on the GPU.  A coordinate
+ * below 0 or NaN is SGDG_EINVAL (no cell contains it); above 1 the last cell
+ * is used, as in cell_index (src/dg_methods.jl:70-78), and its basis
+ * functions vanish there. */
+int sgdg_evaluate(int D, int k, int n, int scheme, const double *coeffs, int64_t npts, const double *xs,
+                  double *values);
+/* The same on device buffers, stream-ordered on `stream` (synchronises it). */
+int sgdg_evaluate_device(int D, int k, int n, int scheme, const double *coeffs_dev, int64_t npts,
+                         const double *xs_dev, double *values_dev, void *stream);
+
 /* Self-test of the device-side bounded wait the persistent kernels use for
  * their dependencies: one thread waits for a counter that nothing increments.
  * Returns SGDG_ETIMEOUT (the expected outcome: the wait gave up, raised the
