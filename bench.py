@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--vlasov-steps", type=int, default=500, help="RK4 steps of the 2x2v Vlasov leg (0: skip)")
     p.add_argument("--serve-requests", type=int, default=32, help="requests in the serving stream (0: skip)")
+    p.add_argument("--eval-points", type=int, default=1 << 20, help="points of the evaluation leg (0: skip)")
     p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the stream, 1/s")
     p.add_argument("--serve-chunk", type=int, default=25, help="max RK4 steps between admissions")
     return p.parse_args()
@@ -300,6 +301,55 @@ def vlasov_leg(sg, stream, steps, batch=16):
 PLAIN_MEASURE_MAX_N = 1_100_000  # larger plain operators take minutes to assemble on the host
 
 
+def evaluate_leg(sg, stream, npts):
+    """Point evaluation (reconstruct_DG) of a 3D sparse k=3, n=7 expansion
+    (seeded Fourier coefficients) at npts uniform points, FP64 on the GPU:
+    device-resident (CUDA events around sgdg_evaluate_device) and end to end
+    through sgdg_evaluate with host buffers; FP64 operations counted per point
+    from the level blocks (k^(D-1) (2k + 2 + D - 1) per block) and the 1D
+    tables (2 k^2 per dimension and level)."""
+    import ctypes
+    import torch
+    Dv, kv, nv = 3, 3, 7
+    rng = np.random.default_rng(21)
+    modes = [(tuple(int(v) for v in rng.integers(1, 4, Dv)), float(rng.uniform(-1, 1)),
+              "sin" if rng.random() < 0.5 else "cos", 0.0) for _ in range(6)]
+    c = sg.fourier_coeffs(Dv, kv, nv, modes)
+    pts = rng.random((npts, Dv))
+    dc = torch.from_numpy(c).to("cuda")
+    dx = torch.from_numpy(pts).to("cuda")
+    dv = torch.empty(npts, dtype=torch.float64, device="cuda")
+    L = sg._lib.lib()
+
+    def run():
+        sg.check(L.sgdg_evaluate_device(Dv, kv, nv, 0, ctypes.c_void_p(dc.data_ptr()), npts,
+                                        ctypes.c_void_p(dx.data_ptr()), ctypes.c_void_p(dv.data_ptr()),
+                                        ctypes.c_void_p(stream.cuda_stream)))
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    reps = 10
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nlev = len({tuple(r) for r in sg.index_map(Dv, kv, nv)[0]})
+    flops = npts * (nlev * kv ** (Dv - 1) * (2 * kv + 2 + Dv - 1) + Dv * (nv + 1) * 2 * kv * kv)
+    t0 = time.perf_counter()
+    vals = sg.reconstruct_DG(Dv, kv, nv, c, pts)
+    e2e = time.perf_counter() - t0
+    return {"workload": "reconstruct_DG, 3D sparse k=3 n=7 expansion at %d uniform points, FP64" % npts,
+            "points": npts, "value": npts / (ms / 1e3), "unit": "points/s", "ms": ms,
+            "fp64_gflops": flops / (ms / 1e3) / 1e9, "fp64_nominal_gflops": 1250.0,
+            "e2e": {"value": npts / e2e, "unit": "points/s", "h2d_bytes": int(c.nbytes + pts.nbytes),
+                    "d2h_bytes": int(vals.nbytes)},
+            "max_abs_diff_device_vs_host_api": float(np.max(np.abs(dv.cpu().numpy() - vals)))}
+
+
 def serving_leg(sg, args):
     """Poisson stream of advection requests of uneven (D, k, n) through the
     request loop (continuous batching), and the same stream through the plain
@@ -531,6 +581,8 @@ def run_ours(args):
         line["vlasov"] = vlasov_leg(sg, stream, args.vlasov_steps)
     if args.serve_requests > 0:
         line["serving"] = serving_leg(sg, args)
+    if args.eval_points > 0:
+        line["evaluate"] = evaluate_leg(sg, stream, args.eval_points)
     if cpu:
         line["cpu_baseline"] = {"value": cpu[0], "unit": UNIT, "cores": cpu[2], "kind": "port",
                                 "sample": "1 solve, %d RK4 steps (%.1f s), FP64 CSR oracle" % (
