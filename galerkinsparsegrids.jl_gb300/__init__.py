@@ -281,6 +281,13 @@ class SparseGridOperator:
         return _csr_from(lambda p: lib().sgdg_op_nnz(self._h, which, p),
                          lambda a, b, c: lib().sgdg_op_export_csr(self._h, which, a, b, c), m)
 
+    def device_csr(self, which):
+        """The operator as the plain form holds it on the device, assembled on
+        the GPU, copied back as scipy CSR (same entries as csr())."""
+        m = self._len(which)
+        return _csr_from(lambda p: lib().sgdg_op_device_nnz(self._h, which, p),
+                         lambda a, b, c: lib().sgdg_op_export_device_csr(self._h, which, a, b, c), m)
+
     def apply(self, x, which=1, method="plain"):
         """y = A x on the GPU (host arrays in and out)."""
         x = np.ascontiguousarray(x, np.float64)

@@ -214,6 +214,73 @@ CSR add_scaled(const std::vector<const CSR*>& As, const std::vector<double>& s) 
     return out;
 }
 
+LineTables line_tables(const DLF1D& op, int levels, bool square) {
+    const int k = op.k;
+    LineTables T;
+    T.k = k;
+    T.levels = levels;
+    std::vector<int64_t> marker;
+    std::vector<double> acc;
+    std::vector<int32_t> cols;
+    for (int lm = 1; lm <= levels; lm++) {
+        const int nrb = 1 << (lm - 1), m = nrb * k;
+        // leading m x m block: the stored blocks of row block rb with column
+        // block < nrb (the admissible levels), in stored order (assemble_dd)
+        std::vector<int64_t> lp(m + 1, 0);
+        std::vector<int32_t> lc;
+        std::vector<double> lv;
+        for (int rb = 0; rb < nrb; rb++)
+            for (int md = 0; md < k; md++) {
+                for (int p = op.rowptr[rb]; p < op.rowptr[rb + 1]; p++) {
+                    const int cb = op.colblk[p];
+                    if (cb >= nrb) continue;
+                    for (int mj = 0; mj < k; mj++) {
+                        lc.push_back(cb * k + mj);
+                        lv.push_back(op.val[(size_t)p * k * k + (size_t)md * k + mj]);
+                    }
+                }
+                lp[rb * k + md + 1] = (int64_t)lc.size();
+            }
+        T.roff.push_back((int64_t)T.rowptr.size());
+        if (!square) {
+            for (int64_t r = 0; r <= m; r++) T.rowptr.push_back((int64_t)T.col.size() + lp[r]);
+            T.col.insert(T.col.end(), lc.begin(), lc.end());
+            T.val.insert(T.val.end(), lv.begin(), lv.end());
+            continue;
+        }
+        // its square, row by row in the order spgemm_sum accumulates (the
+        // row's entries ascending, each times the entries of that row)
+        marker.assign(m, -1);
+        acc.assign(m, 0.0);
+        const int64_t base = (int64_t)T.col.size();
+        T.rowptr.push_back(base);
+        for (int r = 0; r < m; r++) {
+            cols.clear();
+            for (int64_t p = lp[r]; p < lp[r + 1]; p++) {
+                const int32_t j = lc[p];
+                const double a = lv[p];
+                for (int64_t q = lp[j]; q < lp[j + 1]; q++) {
+                    const int32_t c = lc[q];
+                    if (marker[c] != r) {
+                        marker[c] = r;
+                        acc[c] = a * lv[q];
+                        cols.push_back(c);
+                    } else {
+                        acc[c] += a * lv[q];
+                    }
+                }
+            }
+            std::sort(cols.begin(), cols.end());
+            for (int32_t c : cols) {
+                T.col.push_back(c);
+                T.val.push_back(acc[c]);
+            }
+            T.rowptr.push_back((int64_t)T.col.size());
+        }
+    }
+    return T;
+}
+
 // src/pdes.jl:22-49: [[0, I], [lap, 0]]
 CSR wave_rhs(const CSR& lap) {
     const int64_t N = lap.m;

@@ -13,6 +13,7 @@
 #include "device_util.h"
 #include "engine.h"
 #include "api_util.h"
+#include "device_csr.h"
 #include "mf_engine.h"
 #include "sgdg_core.h"
 
@@ -29,65 +30,6 @@ static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
 
 // ------------------------------------------------------- plain form ----
-struct DeviceCSR {
-    DevBuf rowptr, col, val, long_row, long_seg, seg_begin, seg_end, partial;
-    DevCSR d{};
-};
-
-static constexpr int64_t kCsrSplit = 2048;  // entries a row group sums directly
-
-static int pick_vs(const CSR& A) {
-    double avg = A.m ? double(A.nnz()) / double(A.m) : 0.0;
-    if (avg <= 2) return 1;
-    if (avg <= 4) return 2;
-    if (avg <= 10) return 4;
-    if (avg <= 24) return 8;
-    if (avg <= 48) return 16;
-    return 32;
-}
-
-static std::unique_ptr<DeviceCSR> to_device(const CSR& A, cudaStream_t st) {
-    auto D = std::make_unique<DeviceCSR>();
-    D->rowptr = upload(A.rowptr, st);
-    D->col = upload(A.col, st);
-    D->val = upload(A.val, st);
-    D->d.m = A.m;
-    D->d.nnz = A.nnz();
-    D->d.rowptr = D->rowptr.as<int64_t>();
-    D->d.col = D->col.as<int32_t>();
-    D->d.val = D->val.as<double>();
-    D->d.vs = pick_vs(A);
-    // long rows: segments of kCsrSplit entries
-    std::vector<int32_t> lrow, lseg(1, 0);
-    std::vector<int64_t> sb, se;
-    for (int64_t r = 0; r < A.m; r++) {
-        const int64_t b = A.rowptr[r], e = A.rowptr[r + 1];
-        if (e - b <= kCsrSplit) continue;
-        lrow.push_back((int32_t)r);
-        for (int64_t p = b; p < e; p += kCsrSplit) {
-            sb.push_back(p);
-            se.push_back(std::min(e, p + kCsrSplit));
-        }
-        lseg.push_back((int32_t)sb.size());
-    }
-    D->d.split = kCsrSplit;
-    D->d.nlong = (int64_t)lrow.size();
-    D->d.nseg = (int64_t)sb.size();
-    if (!lrow.empty()) {
-        D->long_row = upload(lrow, st);
-        D->long_seg = upload(lseg, st);
-        D->seg_begin = upload(sb, st);
-        D->seg_end = upload(se, st);
-        D->partial.alloc(sizeof(double) * sb.size());
-        D->d.long_row = D->long_row.as<int32_t>();
-        D->d.long_seg = D->long_seg.as<int32_t>();
-        D->d.seg_begin = D->seg_begin.as<int64_t>();
-        D->d.seg_end = D->seg_end.as<int64_t>();
-        D->d.partial = D->partial.as<double>();
-    }
-    return D;
-}
-
 }  // namespace sgdg
 
 using namespace sgdg;
@@ -122,7 +64,7 @@ struct sgdg_op {
     }
     const DevCSR& device(int which) {
         auto it = dev.find(which);
-        if (it == dev.end()) it = dev.emplace(which, to_device(get(which), stream)).first;
+        if (it == dev.end()) it = dev.emplace(which, gpu_operator(ix, *dlf, which, stream)).first;
         return it->second->d;
     }
     ~sgdg_op() {
@@ -373,6 +315,30 @@ int sgdg_op_nnz(sgdg_op* op, int which, int64_t* nnz) {
     API_END
 }
 
+int sgdg_op_device_nnz(sgdg_op* op, int which, int64_t* nnz) {
+    API_BEGIN
+    NEED(op);
+    NEED(nnz);
+    op_stream(op);
+    *nnz = op->device(which).nnz;
+    API_END
+}
+
+int sgdg_op_export_device_csr(sgdg_op* op, int which, int64_t* rowptr, int32_t* col, double* val) {
+    API_BEGIN
+    NEED(op);
+    NEED(rowptr);
+    NEED(col);
+    NEED(val);
+    cudaStream_t st = op_stream(op);
+    op->device(which);
+    const CSR A = download_csr(*op->dev.at(which), st);
+    std::memcpy(rowptr, A.rowptr.data(), sizeof(int64_t) * A.rowptr.size());
+    std::memcpy(col, A.col.data(), sizeof(int32_t) * A.col.size());
+    std::memcpy(val, A.val.data(), sizeof(double) * A.val.size());
+    API_END
+}
+
 int sgdg_op_export_csr(sgdg_op* op, int which, int64_t* rowptr, int32_t* col, double* val) {
     API_BEGIN
     NEED(op);
@@ -421,7 +387,6 @@ int sgdg_apply(sgdg_op* op, int which, int method, const double* x, double* y) {
     NEED(y);
     cudaStream_t st = op_stream(op);
     const int64_t len = which == SGDG_OP_WAVE_RHS ? 2 * op->ix.N : op->ix.N;
-    op->get(which);
     DevBuf dx(sizeof(double) * len), dy(sizeof(double) * len);
     CK(cudaMemcpyAsync(dx.p, x, sizeof(double) * len, cudaMemcpyHostToDevice, st));
     apply_device_impl(op, which, method, dx.as<double>(), dy.as<double>(), st);
@@ -446,17 +411,10 @@ static std::vector<int64_t> out_steps(int64_t nsteps, int nout) {
     return s;
 }
 
-static void plain_evolve(sgdg_op* op, int which_or_adv, const CSR* Aadv, const double* y0, int64_t len, double t0,
-                         double t1, int64_t nsteps, int nout, double* times, double* states) {
+static void plain_evolve(sgdg_op* op, int which_or_adv, const DeviceCSR* Aadv, const double* y0, int64_t len,
+                         double t0, double t1, int64_t nsteps, int nout, double* times, double* states) {
     cudaStream_t st = op_stream(op);
-    std::unique_ptr<DeviceCSR> own;
-    const DevCSR* A;
-    if (Aadv) {
-        own = to_device(*Aadv, st);
-        A = &own->d;
-    } else {
-        A = &op->device(which_or_adv);
-    }
+    const DevCSR* A = Aadv ? &Aadv->d : &op->device(which_or_adv);
     DevBuf y(sizeof(double) * len), acc(sizeof(double) * len), u0(sizeof(double) * len), u1(sizeof(double) * len);
     CK(cudaMemcpyAsync(y.p, y0, sizeof(double) * len, cudaMemcpyHostToDevice, st));
     const double dt = (t1 - t0) / double(nsteps);
@@ -554,14 +512,11 @@ int sgdg_advect_evolve(sgdg_op* op, const double* a, const double* f0, double t0
     check_evolve_args(nsteps, nout, t0, t1);
     const int64_t N = op->ix.N;
     if (method == SGDG_METHOD_PLAIN) {
-        std::vector<const CSR*> v;
+        // -sum_d a_d D_d, assembled on the GPU (the same entries as add_scaled)
         std::vector<double> s;
-        for (int d = 1; d <= op->ix.D; d++) {
-            v.push_back(&op->get(d));
-            s.push_back(-a[d - 1]);
-        }
-        CSR A = add_scaled(v, s);
-        plain_evolve(op, 0, &A, f0, N, t0, t1, nsteps, nout, times, states);
+        for (int d = 1; d <= op->ix.D; d++) s.push_back(-a[d - 1]);
+        auto A = gpu_scaled_sum(op->ix, *op->dlf, s.data(), op_stream(op));
+        plain_evolve(op, 0, A.get(), f0, N, t0, t1, nsteps, nout, times, states);
     } else if (method == SGDG_METHOD_MATFREE) {
         mf_evolve(op, MF_KIND_ADVECT, a, f0, N, t0, t1, nsteps, nout, times, states);
     } else {

@@ -96,4 +96,21 @@ std::vector<Pencil> make_pencils(const SparseIndex& ix, int d) {
     return out;
 }
 
+void pencil_rows(const Pencil& p, int k, int64_t kD, std::vector<int32_t>& out) {
+    int64_t kd1 = 1;
+    for (int q = 0; q < p.d; q++) kd1 *= k;
+    const int nrb = 1 << (p.lmax - 1);
+    for (int rb = 0; rb < nrb; rb++) {
+        // row block rb of the pencil's 1D prefix: level l, cell cd0 within the level
+        int l = 1;
+        while (l < 32 && (rb >> (l - 1)) != 0) l++;
+        const int64_t cd0 = l >= 2 ? rb - (1 << (l - 2)) : 0;
+        const int lc = l > 2 ? l - 2 : 0;
+        for (int i = 0; i < k; i++) {
+            out.push_back((int32_t)(p.blockoff[l - 1] + kD * (cd0 << p.lp) + i * kd1));
+            out.push_back(lc);
+        }
+    }
+}
+
 }  // namespace sgdg

@@ -145,6 +145,24 @@ struct Pencil {
     std::vector<int64_t> blockoff;  // offset of level block (L_-d, l), l = 1..lmax
 };
 std::vector<Pencil> make_pencils(const SparseIndex& ix, int d);
+// Appends, for every row (row block rb, mode i along d) of the pencil's 1D
+// prefix, the pair (row offset, lc): element (row, column) of the pencil sits
+// at row offset + a + (b << lc), with (a, b) the column's low and high parts
+// (lc = log2 of the row level's cell count).
+void pencil_rows(const Pencil& p, int k, int64_t kD, std::vector<int32_t>& out);
+
+// The line operators of the pencils, for every line of lm = 1..levels levels
+// (m = k 2^(lm-1) elements): the leading m x m block of the 1D operator, or
+// its square (accumulated as spgemm_sum does, so the values are the same),
+// as CSR over the line's 1D element index with sorted rows.  Table lm starts
+// at rowptr[roff[lm-1]]; its row pointers index col/val directly.
+struct LineTables {
+    int k = 0, levels = 0;
+    std::vector<int64_t> roff, rowptr;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+};
+LineTables line_tables(const DLF1D& op, int levels, bool square);
 
 void set_error(const std::string& msg);
 }  // namespace sgdg

@@ -84,6 +84,12 @@ int sgdg_op_size(const sgdg_op *op, int64_t *N);
 int sgdg_op_nnz(sgdg_op *op, int which, int64_t *nnz);
 /* The assembled operator as CSR (rowptr: rows+1 entries; columns sorted). */
 int sgdg_op_export_csr(sgdg_op *op, int which, int64_t *rowptr, int32_t *col, double *val);
+/* The same operator as the plain form holds it on the device, assembled on
+ * the GPU (D_d from the pencils' leading 1D blocks, the Laplacian from their
+ * squares merged over d, the wave right-hand side around it): stored entries
+ * and values equal to sgdg_op_export_csr's.  nnz, then the host copy. */
+int sgdg_op_device_nnz(sgdg_op *op, int which, int64_t *nnz);
+int sgdg_op_export_device_csr(sgdg_op *op, int which, int64_t *rowptr, int32_t *col, double *val);
 
 /* y = A x for operator `which` -- the RHS closure (t,x)->*(RHS,x) of
  * src/pdes.jl:63.  Host buffers (length N, or 2N for SGDG_OP_WAVE_RHS).
