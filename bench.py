@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--vlasov-steps", type=int, default=500, help="RK4 steps of the 2x2v Vlasov leg (0: skip)")
     p.add_argument("--serve-requests", type=int, default=32, help="requests in the serving stream (0: skip)")
     p.add_argument("--eval-points", type=int, default=1 << 20, help="points of the evaluation leg (0: skip)")
+    p.add_argument("--assembly", type=int, default=1, help="time GPU vs host operator assembly (0: skip)")
     p.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrival rate of the stream, 1/s")
     p.add_argument("--serve-chunk", type=int, default=25, help="max RK4 steps between admissions")
     return p.parse_args()
@@ -350,6 +351,26 @@ def evaluate_leg(sg, stream, npts):
             "max_abs_diff_device_vs_host_api": float(np.max(np.abs(dv.cpu().numpy() - vals)))}
 
 
+def assembly_leg(sg, D=4, k=3, n=7):
+    """Time to the plain form's wave right-hand side [[0, I], [L, 0]] with
+    L = sum_d D_d D_d for a 4D sparse k=3, n=7 grid (327,888 DOF): assembled
+    on the GPU (the operator the plain evolvers use) and on the host (CSR
+    products, the exported operator); both hold the same entries."""
+    L = sg._lib.lib()
+    import ctypes
+    op = sg.SparseGridOperator(D, k, n)
+    z = ctypes.c_int64()
+    t0 = time.perf_counter()
+    sg.check(L.sgdg_op_device_nnz(op._h, -1, ctypes.byref(z)))
+    gpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nnz_host = op.nnz(-1)
+    host_s = time.perf_counter() - t0
+    op.close()
+    return {"workload": "wave RHS of the plain form, %dD sparse k=%d n=%d (%d DOF)" % (D, k, n, sg.get_size(D, k, n)),
+            "nnz": int(z.value), "gpu_s": gpu_s, "host_s": host_s, "same_nnz": int(z.value) == int(nnz_host)}
+
+
 def serving_leg(sg, args):
     """Poisson stream of advection requests of uneven (D, k, n) through the
     request loop (continuous batching), and the same stream through the plain
@@ -581,6 +602,8 @@ def run_ours(args):
         line["vlasov"] = vlasov_leg(sg, stream, args.vlasov_steps)
     if args.serve_requests > 0:
         line["serving"] = serving_leg(sg, args)
+    if args.assembly:
+        line["assembly"] = assembly_leg(sg)
     if args.eval_points > 0:
         line["evaluate"] = evaluate_leg(sg, stream, args.eval_points)
     if cpu:
