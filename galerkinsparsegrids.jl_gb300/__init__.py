@@ -668,6 +668,25 @@ class Batch:
         """All live states into host memory at address ``ptr`` (synchronises)."""
         check(lib().sgdg_batch_download(self._h, ctypes.c_void_p(ptr)))
 
+    def step_host(self, y_in, y_out=None, nsteps=1, chunks=8):
+        """Every live state from host memory, ``nsteps`` RK4 steps, the results
+        back (id order, like upload/download).  ``y_in`` / ``y_out`` are
+        addresses of float64 host memory (pinned for the copies to overlap the
+        steps) or numpy arrays; ``y_out`` defaults to ``y_in``."""
+        keep = []
+
+        def addr(a):
+            if isinstance(a, np.ndarray):
+                if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != self.total_size():
+                    raise ValueError("need a C-contiguous float64 array of total_size() entries")
+                keep.append(a)
+                return a.ctypes.data
+            return int(a)
+        pin = addr(y_in)
+        pout = pin if y_out is None else addr(y_out)
+        check(lib().sgdg_batch_step_host(self._h, ctypes.c_void_p(pin), ctypes.c_void_p(pout), int(nsteps),
+                                         int(chunks)))
+
     def autotune(self):
         """Tunes the tile shape of every (D, k) in the batch not tuned yet;
         returns how many were tuned."""

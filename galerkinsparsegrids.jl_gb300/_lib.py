@@ -22,7 +22,7 @@ EXPORTS = [
     "sgdg_advect_evolve",
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
-    "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_info", "sgdg_batch_autotune",
+    "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_host", "sgdg_batch_step_info", "sgdg_batch_autotune",
     "sgdg_batch_add_vlasov",
     "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes",
     "sgdg_transform_1d_nnz", "sgdg_transform_1d_export", "sgdg_transform_nnz", "sgdg_transform_export",
@@ -130,6 +130,7 @@ def lib(build=True):
     _sig(L, "sgdg_batch_total_size", [_vp, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_batch_upload", [_vp, _vp])
     _sig(L, "sgdg_batch_download", [_vp, _vp])
+    _sig(L, "sgdg_batch_step_host", [_vp, _vp, _vp, _c64, _ci])
     _sig(L, "sgdg_batch_step_info", [_vp, ctypes.POINTER(_c64), ctypes.POINTER(_cd)])
     _sig(L, "sgdg_set_hbm_budget", [_c64])
     _sig(L, "sgdg_hbm_in_use", [ctypes.POINTER(_c64)])

@@ -889,6 +889,15 @@ int sgdg_batch_download(sgdg_batch* b, double* y_all) {
     API_END
 }
 
+int sgdg_batch_step_host(sgdg_batch* b, const double* y_in, double* y_out, int64_t nsteps, int nchunks) {
+    API_BEGIN
+    NEED(b);
+    NEED(y_in);
+    NEED(y_out);
+    b->eng.step_host(y_in, y_out, nsteps, nchunks);
+    API_END
+}
+
 int sgdg_batch_step_info(sgdg_batch* b, int64_t* launches, double* dofs) {
     API_BEGIN
     NEED(b);

@@ -38,6 +38,14 @@ void MFEngine::set_stream(cudaStream_t st) {
 void MFEngine::drop_graph() {
     if (graph_) cudaGraphExecDestroy(graph_);
     graph_ = nullptr;
+    for (Chunk& c : chunks_) {
+        if (c.graph) cudaGraphExecDestroy(c.graph);
+        if (c.st) {
+            cudaStreamSynchronize(c.st);
+            cudaStreamDestroy(c.st);
+        }
+    }
+    chunks_.clear();
 }
 
 MFEngine::Solve& MFEngine::at(int id) {
@@ -371,7 +379,8 @@ void MFEngine::plan() {
 // wavefront earlier and is normally complete: CTAs rarely wait, while the
 // groups in flight (about one per phase) keep their reused vectors in L2.
 void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only,
-                           const std::map<std::pair<int, int>, MFTile>* shapes) {
+                           const std::map<std::pair<int, int>, MFTile>* shapes, int chunk, int nchunks,
+                           std::vector<std::array<int, 3>>* ranges) {
     struct Group {
         std::vector<std::vector<MFItem>> phases;
     };
@@ -398,8 +407,11 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
             (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
         int kDm1 = 1;
         for (int q = 0; q < D - 1; q++) kDm1 *= k;
+        const int ng = (ns + gs - 1) / gs;
         for (int s0 = 0; s0 < ns; s0 += gs) {
             const int s1 = std::min(ns, s0 + gs);
+            if ((int64_t)(s0 / gs) * nchunks / ng != chunk) continue;  // another chunk's group
+            if (ranges) ranges->push_back({(int)ci, s0, s1 - s0});
             Group grp;
             // one phase: tiles of every pencil along d over the group's slots
             auto phase = [&](int d, int tab, int src, int dst, int flags, int wsel) {
@@ -648,6 +660,105 @@ void MFEngine::capture() {
     }
 }
 
+void MFEngine::build_chunks(int nchunks) {
+    if ((int)chunks_.size() == nchunks) return;  // chunks_ is dropped with the graph on a re-plan
+    for (Chunk& c : chunks_) {
+        if (c.graph) cudaGraphExecDestroy(c.graph);
+        if (c.st) {
+            cudaStreamSynchronize(c.st);
+            cudaStreamDestroy(c.st);
+        }
+    }
+    chunks_.clear();
+    chunks_.resize(nchunks);
+    const size_t smem = smem_;
+    const int tb = table_bytes_;
+    for (int ci = 0; ci < nchunks; ci++) {
+        Chunk& ch = chunks_[ci];
+        std::vector<MFItem> items;
+        int nctr = 0;
+        build_items(items, nctr, false, nullptr, ci, nchunks, &ch.ranges);
+        smem_ = smem;  // build_items sized the launch for this chunk only; keep the whole list's
+        table_bytes_ = tb;
+        CK(cudaStreamCreateWithFlags(&ch.st, cudaStreamNonBlocking));
+        ch.nitems = (int)items.size();
+        ch.nctr = nctr;
+        if (ch.nitems == 0) continue;
+        ch.items = upload(items, ch.st);
+        ch.ctr.alloc(sizeof(int) * (size_t)std::max(nctr, 1));
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(ch.st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t err = cudaSuccess;
+        for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
+            err = launch_mf_stage(ch.items.as<MFItem>(), ch.nitems, classes_d_.as<MFClass>(), ch.ctr.as<int>(), ch.nctr,
+                                  stage, (stage - 1) % 2, err_d_.as<int>(), smem_, table_bytes_, grid_, ch.st);
+        cudaError_t e2 = cudaStreamEndCapture(ch.st, &g);
+        if (err != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            throw Error(SGDG_ECUDA, std::string("graph capture: ") + cudaGetErrorString(err != cudaSuccess ? err : e2));
+        }
+        cudaError_t e3 = cudaGraphInstantiate(&ch.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) {
+            ch.graph = nullptr;
+            throw Error(SGDG_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+        }
+    }
+    for (Chunk& ch : chunks_) CK(cudaStreamSynchronize(ch.st));
+}
+
+void MFEngine::step_host(const double* in, double* out, int64_t nsteps, int nchunks) {
+    plan();
+    if (nsteps < 0) throw Error(SGDG_EINVAL, "nsteps must be >= 0");
+    nchunks = std::max(1, std::min(nchunks, 64));
+    build_chunks(nchunks);
+    std::vector<int64_t> off(solves_.size(), -1);  // host offset of every live id
+    int64_t o = 0;
+    for (size_t id = 0; id < solves_.size(); id++)
+        if (solves_[id].live) {
+            off[id] = o;
+            o += solves_[id].Ns;
+        }
+    cudaEvent_t ready;
+    CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(ready, stream_));  // after the engine stream's earlier work
+    // copies of a chunk's slots: runs that are consecutive both on the device
+    // and on the host
+    auto copies = [&](const Chunk& ch, bool h2d) {
+        for (const auto& r : ch.ranges) {
+            const ClassArena& c = *classes_[r[0]];
+            for (int s = r[1]; s < r[1] + r[2];) {
+                const int64_t h = off[c.slots[s]];
+                int run = 1;
+                while (s + run < r[1] + r[2] && off[c.slots[s + run]] == h + (int64_t)run * c.Ns) run++;
+                double* dv = c.y.as<double>() + (size_t)s * c.Ns;
+                const size_t bytes = sizeof(double) * (size_t)c.Ns * run;
+                if (h2d)
+                    CK(cudaMemcpyAsync(dv, in + h, bytes, cudaMemcpyHostToDevice, ch.st));
+                else
+                    CK(cudaMemcpyAsync(out + h, dv, bytes, cudaMemcpyDeviceToHost, ch.st));
+                s += run;
+            }
+        }
+    };
+    for (Chunk& ch : chunks_) {
+        if (ch.ranges.empty()) continue;
+        CK(cudaStreamWaitEvent(ch.st, ready, 0));
+        copies(ch, true);
+        for (const auto& r : ch.ranges) {
+            const ClassArena& c = *classes_[r[0]];
+            CK(launch_f64_to_f32(c.y.as<double>() + (size_t)r[1] * c.Ns, c.u0.as<float>() + (size_t)r[1] * c.Ns,
+                                 (int64_t)r[2] * c.Ns, ch.st));
+        }
+        if (ch.graph)
+            for (int64_t i = 0; i < nsteps; i++) CK(cudaGraphLaunch(ch.graph, ch.st));
+        copies(ch, false);
+    }
+    for (Chunk& ch : chunks_) CK(cudaStreamSynchronize(ch.st));
+    CK(cudaEventDestroy(ready));
+    if (check_error() != SGDG_OK) throw Error(SGDG_ETIMEOUT, "a bounded device wait gave up; state is unreliable");
+}
+
 void MFEngine::step(int64_t nsteps) {
     plan();
     if (nitems_ == 0 || nsteps <= 0) return;
@@ -693,13 +804,24 @@ void MFEngine::set_state(int id, const double* host) {
 void MFEngine::upload_all(const double* host) {
     plan();
     int64_t off = 0;
-    for (int id = 0; id < (int)solves_.size(); id++) {
+    int id = 0;
+    const int n = (int)solves_.size();
+    while (id < n) {
+        if (!solves_[id].live) {
+            id++;
+            continue;
+        }
+        // one copy for a run of ids that sit in consecutive slots of one class
         const Solve& s = solves_[id];
-        if (!s.live) continue;
         const ClassArena& c = *classes_[s.cls];
-        CK(cudaMemcpyAsync(c.y.as<double>() + (size_t)s.slot * c.Ns, host + off, sizeof(double) * c.Ns,
+        int run = 1;
+        while (id + run < n && solves_[id + run].live && solves_[id + run].cls == s.cls &&
+               solves_[id + run].slot == s.slot + run)
+            run++;
+        CK(cudaMemcpyAsync(c.y.as<double>() + (size_t)s.slot * c.Ns, host + off, sizeof(double) * c.Ns * run,
                            cudaMemcpyHostToDevice, stream_));
-        off += s.Ns;
+        off += (int64_t)run * c.Ns;
+        id += run;
     }
     for (auto& cp : classes_)
         CK(launch_f64_to_f32(cp->y.as<double>(), cp->u0.as<float>(), (int64_t)cp->slots.size() * cp->Ns, stream_));

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <map>
 #include <memory>
 #include <tuple>
@@ -50,6 +51,12 @@ class MFEngine {
     void set_state(int id, const double* host); // async (pageable memory is staged)
     void upload_all(const double* host);
     void download_all(double* host);
+    // Every live state from host_in (id order, like upload_all), nsteps RK4
+    // steps, the results to host_out (may equal host_in); synchronises.  The
+    // groups are split into nchunks chunks, each with its own work list,
+    // counters, graph and stream, so one chunk's copies overlap the others'
+    // steps.  Host memory should be pinned for the copies to overlap.
+    void step_host(const double* host_in, double* host_out, int64_t nsteps, int nchunks);
 
     // apply mode (single solve): y_dev = op(x_dev)
     void apply(const double* x_dev, double* y_dev);
@@ -92,8 +99,11 @@ class MFEngine {
     };
 
     void plan();
+    // chunk / nchunks: only the groups of that chunk (each class's groups cut
+    // into nchunks contiguous runs); ranges receives (class, first slot, slots)
     void build_items(std::vector<MFItem>& items, int& nctr, bool pass_only = false,
-                     const std::map<std::pair<int, int>, MFTile>* shapes = nullptr);
+                     const std::map<std::pair<int, int>, MFTile>* shapes = nullptr, int chunk = 0, int nchunks = 1,
+                     std::vector<std::array<int, 3>>* ranges = nullptr);
     const STable& stab(int k, int n);
     const TTables& ttab(int k, int n);
     void capture();
@@ -113,6 +123,15 @@ class MFEngine {
     int table_bytes_ = 0;  // shared-memory operator table reserved ahead of the tile
     bool dirty_ = true;
     cudaGraphExec_t graph_ = nullptr;
+    struct Chunk {  // step_host's pipeline stage
+        DevBuf items, ctr;
+        int nitems = 0, nctr = 0;
+        cudaStream_t st = nullptr;
+        cudaGraphExec_t graph = nullptr;
+        std::vector<std::array<int, 3>> ranges;  // (class, first slot, slots)
+    };
+    std::vector<Chunk> chunks_;
+    void build_chunks(int nchunks);
 };
 
 }  // namespace sgdg

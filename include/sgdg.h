@@ -194,6 +194,12 @@ int sgdg_batch_upload(sgdg_batch *b, const double *y_all);
 /* Copies every live solve's state into one host array (same order) and
  * synchronises the batch stream. */
 int sgdg_batch_download(sgdg_batch *b, double *y_all);
+/* Host states in, RK4 steps, host states out (same layout as upload/download;
+ * y_out may equal y_in), in one call that synchronises.  The batch's groups
+ * of solves are split into nchunks pipeline chunks on their own streams, so
+ * one chunk's host<->device copies overlap the other chunks' steps; pinned
+ * host memory is needed for the copies to overlap. */
+int sgdg_batch_step_host(sgdg_batch *b, const double *y_in, double *y_out, int64_t nsteps, int nchunks);
 /* Autotuner: for every (D, k) of the batch's solves that has no tuned tile
  * shape yet, times one RK stage's pencil tiles of the whole batch for each
  * candidate shape (tile width factor 2^wlog, wlog -2..3, x warp-cooperative

@@ -1,0 +1,45 @@
+"""Batch.step_host: host states in, RK4 steps, host states out, with the
+batch's groups split into pipeline chunks on their own streams.  Each chunk
+runs the same tiles as the whole batch, so the states must equal (bitwise)
+upload + step + download, for any chunk count and with solves of several
+classes added in interleaved order."""
+import numpy as np
+import pytest
+
+
+def mixed_batch(sgdg):
+    rng = np.random.default_rng(12)
+    b = sgdg.Batch()
+    specs = []
+    for i in range(14):
+        if i % 3 == 0:
+            N = sgdg.get_size(3, 3, 4)
+            y0 = np.concatenate([sgdg.fourier_coeffs(3, 3, 4, [((1, 2, 1), 0.5, "sin", 0.0)]), np.zeros(N)])
+            b.add("wave", 3, 3, 4, y0, 2e-3)
+        else:
+            y0 = rng.standard_normal(sgdg.get_size(2, 2, 5)) * 0.1
+            b.add("advect", 2, 2, 5, y0, 1e-3, a=[0.6, -0.2 * i])
+        specs.append(y0)
+    return b, np.concatenate(specs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("chunks", [1, 2, 3, 8])
+def test_step_host_equals_upload_step_download(sgdg, chunks):
+    b, y = mixed_batch(sgdg)
+    ref = y.copy()
+    b.upload(ref.ctypes.data)
+    b.step(3)
+    b.download(ref.ctypes.data)
+    b2, y2 = mixed_batch(sgdg)
+    out = np.empty_like(y2)
+    b2.step_host(y2, out, nsteps=3, chunks=chunks)
+    assert np.array_equal(out, ref)
+    # in place, twice: the same as six steps
+    b2.step_host(y2, nsteps=3, chunks=chunks)
+    b2.step_host(y2, nsteps=3, chunks=chunks)
+    b.step(3)
+    b.download(ref.ctypes.data)
+    assert np.array_equal(y2, ref)
+    b.close()
+    b2.close()
