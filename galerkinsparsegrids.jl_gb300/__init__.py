@@ -191,9 +191,24 @@ def _i1d(k, L, C, M):
     return k * (start + C - 1) + M - 1
 
 
-def tensor_construct(D, k, n, vcoeff_array, scheme="sparse"):
+def _tensor_sum(D, k, n, Z, coef, scheme):
+    """sum_t amp_t part_t(e^{i phi_t} prod_d Z[t, d][i_d]) on the GPU."""
+    Zc = np.ascontiguousarray(np.asarray(Z, np.complex128))
+    if Zc.ndim != 3 or Zc.shape[1:] != (D, k << n):
+        raise ValueError("Z must be (terms, D, k 2^n)")
+    out = np.empty(get_size(D, k, n, scheme))
+    c = np.ascontiguousarray(coef, np.float64)
+    check(lib().sgdg_tensor_sum(D, k, n, _scheme(scheme), Zc.shape[0], Zc.view(np.float64).reshape(-1),
+                                c.reshape(-1), out))
+    return out
+
+
+def tensor_construct(D, k, n, vcoeff_array, scheme="sparse", device=False):
     """Coefficients of prod_d f_d(x_d) from 1D coefficient vectors
-    (src/tensor_construct.jl:57-63)."""
+    (src/tensor_construct.jl:57-63); ``device=True`` computes them on the GPU."""
+    if device:
+        Z = np.asarray([np.asarray(v, np.float64) for v in vcoeff_array])[None].astype(np.complex128)
+        return _tensor_sum(D, k, n, Z, [[1.0, 1.0, 0.0, 0.0]], scheme)
     L, C, M = index_map(D, k, n, scheme)
     out = np.ones(L.shape[0])
     for q in range(D):
@@ -201,9 +216,18 @@ def tensor_construct(D, k, n, vcoeff_array, scheme="sparse"):
     return out
 
 
-def fourier_coeffs(D, k, n, modes, scheme="sparse"):
+def fourier_coeffs(D, k, n, modes, scheme="sparse", device=False):
     """Coefficients of sum_m amp * trig(2 pi a.x + phase), exactly separable:
-    ``modes`` = [(a (D ints), amp, "sin"|"cos", phase), ...]."""
+    ``modes`` = [(a (D ints), amp, "sin"|"cos", phase), ...].  The 1D
+    projections are computed on the host; ``device=True`` builds the D-dim
+    vector from them on the GPU."""
+    if device:
+        Z = np.asarray([[_fourier_1d(k, n, int(a[q])) for q in range(D)] for a, _, _, _ in modes])
+        coef = []
+        for a, amp, kind, ph in modes:
+            z0 = np.exp(1j * ph)
+            coef.append([amp, z0.real, z0.imag, 0.0 if kind == "cos" else 1.0])
+        return _tensor_sum(D, k, n, Z, coef, scheme)
     idx = _index_1d(D, k, n, scheme)
     out = np.zeros(idx[0].shape[0])
     for a, amp, kind, ph in modes:

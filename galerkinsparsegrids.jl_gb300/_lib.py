@@ -31,7 +31,7 @@ EXPORTS = [
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
     "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
     "sgdg_server_counts",
-    "sgdg_evaluate", "sgdg_evaluate_device", "sgdg_selftest_bounded_wait", "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
+    "sgdg_evaluate", "sgdg_evaluate_device", "sgdg_tensor_sum", "sgdg_selftest_bounded_wait", "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
 ]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
 
@@ -102,6 +102,7 @@ def lib(build=True):
     _sig(L, "sgdg_batch_add_vlasov", [_vp, _ci, _ci, _ci, _ci, _cd, _f64p, _f64p, ctypes.POINTER(_ci)])
     _sig(L, "sgdg_evaluate", [_ci, _ci, _ci, _ci, _f64p, _c64, _f64p, _f64p])
     _sig(L, "sgdg_evaluate_device", [_ci, _ci, _ci, _ci, _vp, _c64, _vp, _vp, _vp])
+    _sig(L, "sgdg_tensor_sum", [_ci, _ci, _ci, _ci, _ci, _f64p, _f64p, _f64p])
     _sig(L, "sgdg_selftest_bounded_wait", [ctypes.POINTER(_cd)])
     _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_server_destroy", [_vp])

@@ -115,6 +115,57 @@ __global__ void __launch_bounds__(32 * kEvalWarps)
     }
 }
 
+// Sum over terms of separable products (tensor_construct,
+// src/tensor_construct.jl:19-62, and sums of Fourier modes): coefficient i
+// of the D-dim vector is  sum_t amp_t * part_t( e^{i phi_t} prod_d Z_td[i_d] )
+// with i_d the 1D index of i along d (get_index_1D,
+// src/additional_tools.jl:8-13: k * (block of (level, cell)) + mode) and
+// part_t the real or imaginary part.  The complex products round each
+// product and sum separately, as numpy does.  One thread per coefficient.
+struct TermShape {
+    int D, k, nlev, nterms;
+    int64_t kD, N1, N;
+    const int8_t* levels;
+    const int32_t* lev_off;
+    const double* Z;      // nterms x D x N1 (re, im)
+    const double* coef;   // nterms x 4: amp, cos phi, sin phi, part (0 real, 1 imaginary)
+};
+
+__global__ void k_tensor_sum(TermShape S, double* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    int lo = 0, hi = S.nlev - 1;
+    while (lo < hi) {  // level block holding i
+        const int mid = (lo + hi + 1) >> 1;
+        if (S.lev_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const int8_t* L = S.levels + (size_t)lo * S.D;
+    const int64_t local = i - S.lev_off[lo];
+    int64_t cl = local / S.kD, ml = local - cl * S.kD;
+    int64_t i1[8];
+    for (int d = 0; d < S.D; d++) {
+        const int64_t nc = (int64_t)1 << (L[d] > 2 ? L[d] - 2 : 0);
+        const int64_t c = cl % nc, m = ml % S.k;
+        cl /= nc;
+        ml /= S.k;
+        i1[d] = S.k * ((L[d] >= 2 ? ((int64_t)1 << (L[d] - 2)) : 0) + c) + m;
+    }
+    double acc = 0.0;
+    for (int t = 0; t < S.nterms; t++) {
+        const double* cf = S.coef + 4 * t;
+        double zr = cf[1], zi = cf[2];
+        for (int d = 0; d < S.D; d++) {
+            const double* z = S.Z + (((size_t)t * S.D + d) * S.N1 + i1[d]) * 2;
+            const double ar = __dsub_rn(__dmul_rn(zr, z[0]), __dmul_rn(zi, z[1]));
+            const double ai = __dadd_rn(__dmul_rn(zr, z[1]), __dmul_rn(zi, z[0]));
+            zr = ar;
+            zi = ai;
+        }
+        acc = __dadd_rn(acc, __dmul_rn(cf[0], cf[3] != 0.0 ? zi : zr));
+    }
+    out[i] = acc;
+}
+
 // device tables of one (D, k, n, scheme)
 struct EvalTables {
     SparseIndex ix;
@@ -182,6 +233,16 @@ void evaluate_impl(int D, int k, int n, int scheme, const double* coeffs, int64_
     if (h_err) throw Error(SGDG_EINVAL, "a point coordinate is below 0 or NaN (no cell contains it)");
 }
 
+void tensor_sum_impl(int D, int k, int n, int scheme, int nterms, const double* Z, const double* coef, double* out,
+                     cudaStream_t st) {
+    const EvalTables& T = eval_tables(D, k, n, scheme);
+    TermShape S{D, k, T.ix.nlev, nterms, T.ix.kD, (int64_t)k << n, T.ix.N, T.levels.as<int8_t>(),
+                T.lev_off.as<int32_t>(), Z, coef};
+    k_tensor_sum<<<(int)((T.ix.N + 255) / 256), 256, 0, st>>>(S, out);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+}
+
 void check_shape(int D, int k, int n) {
     if (D < 1 || D > 8) throw Error(SGDG_EINVAL, "D must be in 1..8");
     if (k < 1 || k > kKMax) throw Error(SGDG_EINVAL, "k must be in 1..10");
@@ -213,6 +274,26 @@ int sgdg_evaluate(int D, int k, int n, int scheme, const double* coeffs, int64_t
     CK(cudaMemcpyAsync(dx.p, xs, sizeof(double) * (size_t)npts * D, cudaMemcpyHostToDevice, st));
     evaluate_impl(D, k, n, scheme, dc.as<double>(), npts, dx.as<double>(), dv.as<double>(), st);
     CK(cudaMemcpyAsync(values, dv.p, sizeof(double) * (size_t)npts, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    API_END
+}
+
+int sgdg_tensor_sum(int D, int k, int n, int scheme, int nterms, const double* Z, const double* coef, double* out) {
+    API_BEGIN
+    check_shape(D, k, n);
+    if (nterms < 1) throw Error(SGDG_EINVAL, "nterms must be >= 1");
+    NEED(Z);
+    NEED(coef);
+    NEED(out);
+    require_gpu();
+    const SparseIndex& ix = eval_tables(D, k, n, scheme).ix;
+    const size_t zlen = (size_t)nterms * D * ((size_t)k << n) * 2;
+    cudaStream_t st = nullptr;
+    DevBuf dz(sizeof(double) * zlen), dc(sizeof(double) * 4 * (size_t)nterms), dout(sizeof(double) * ix.N);
+    CK(cudaMemcpyAsync(dz.p, Z, sizeof(double) * zlen, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dc.p, coef, sizeof(double) * 4 * nterms, cudaMemcpyHostToDevice, st));
+    tensor_sum_impl(D, k, n, scheme, nterms, dz.as<double>(), dc.as<double>(), dout.as<double>(), st);
+    CK(cudaMemcpyAsync(out, dout.p, sizeof(double) * ix.N, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     API_END
 }

@@ -269,6 +269,15 @@ int sgdg_server_counts(sgdg_server *s, int64_t *queued, int64_t *running, int64_
  * functions vanish there. */
 int sgdg_evaluate(int D, int k, int n, int scheme, const double *coeffs, int64_t npts, const double *xs,
                   double *values);
+/* Sum of separable terms, computed on the GPU: coefficient i of the D-dim
+ * vector is sum_t amp_t * part_t(e^{i phi_t} prod_d Z_td[i_d]) with i_d the
+ * 1D index of i along d (get_index_1D, src/additional_tools.jl:8-13).  Z holds
+ * nterms x D complex 1D coefficient vectors of k 2^n entries, (re, im)
+ * interleaved; coef holds per term (amp, cos phi, sin phi, part), part 0 for
+ * the real and 1 for the imaginary part.  One real term of real vectors is
+ * tensor_construct (src/tensor_construct.jl:19-62); sums of modes
+ * exp(2 pi i a.x) give Fourier initial conditions. */
+int sgdg_tensor_sum(int D, int k, int n, int scheme, int nterms, const double *Z, const double *coef, double *out);
 /* The same on device buffers, stream-ordered on `stream` (synchronises it). */
 int sgdg_evaluate_device(int D, int k, int n, int scheme, const double *coeffs_dev, int64_t npts,
                          const double *xs_dev, double *values_dev, void *stream);
