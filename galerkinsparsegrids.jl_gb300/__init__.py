@@ -435,11 +435,22 @@ def transform_1D(k, n, frm, to):
                      lambda a, b, c: L.sgdg_transform_1d_export(k, n, w, a, b, c), k << n)
 
 
-def transform(D, k, n, frm, to, scheme="sparse"):
-    """transform(D, k, n, from, to) (src/multidim_nodal_basis.jl:83-124), CSR."""
+def transform(D, k, n, frm, to, scheme="sparse", device=False):
+    """transform(D, k, n, from, to) (src/multidim_nodal_basis.jl:83-124), CSR;
+    ``device=True`` assembles it on the GPU (the same entries and values)."""
     w = _transform_id(frm, to)
     sc = _scheme(scheme)
     L = lib()
+    if device:
+        nnz = ctypes.c_int64()
+        check(L.sgdg_transform_device_export(D, k, n, sc, w, ctypes.byref(nnz), None, None, None))
+        N = get_size(D, k, n, scheme)
+        rp = np.empty(N + 1, np.int64)
+        cl = np.empty(nnz.value, np.int32)
+        vl = np.empty(nnz.value, np.float64)
+        check(L.sgdg_transform_device_export(D, k, n, sc, w, ctypes.byref(nnz), rp.ctypes.data_as(ctypes.c_void_p),
+                                             cl.ctypes.data_as(ctypes.c_void_p), vl.ctypes.data_as(ctypes.c_void_p)))
+        return sp.csr_matrix((vl, cl, rp), shape=(N, N))
     return _csr_from(lambda p: L.sgdg_transform_nnz(D, k, n, sc, w, p),
                      lambda a, b, c: L.sgdg_transform_export(D, k, n, sc, w, a, b, c), get_size(D, k, n, scheme))
 

@@ -26,6 +26,7 @@ EXPORTS = [
     "sgdg_batch_add_vlasov",
     "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes",
     "sgdg_transform_1d_nnz", "sgdg_transform_1d_export", "sgdg_transform_nnz", "sgdg_transform_export",
+    "sgdg_transform_device_export",
     "sgdg_vlasov_create", "sgdg_vlasov_destroy", "sgdg_vlasov_size", "sgdg_vlasov_v_point",
     "sgdg_vlasov_transform_nnz", "sgdg_vlasov_transform_export", "sgdg_vlasov_rhs", "sgdg_vlasov_evolve",
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
@@ -91,6 +92,7 @@ def lib(build=True):
     _sig(L, "sgdg_transform_1d_export", [_ci, _ci, _ci, _i64p, _i32p, _f64p])
     _sig(L, "sgdg_transform_nnz", [_ci, _ci, _ci, _ci, _ci, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_transform_export", [_ci, _ci, _ci, _ci, _ci, _i64p, _i32p, _f64p])
+    _sig(L, "sgdg_transform_device_export", [_ci, _ci, _ci, _ci, _ci, ctypes.POINTER(_c64), _vp, _vp, _vp])
     _sig(L, "sgdg_vlasov_create", [_ci, _ci, _ci, _ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_vlasov_destroy", [_vp])
     _sig(L, "sgdg_vlasov_size", [_vp, ctypes.POINTER(_c64)])

@@ -78,12 +78,17 @@ struct sgdg_op {
 // Operators of vlasov_evolve (src/pdes.jl:131-227) for D space dimensions:
 // phase space of P = 2D dimensions (x_1..x_D, p_1..p_D), grad_matrix(P), the
 // four nodal transforms and the velocity points v_d = n2p m2n (2 p_d - 1).
+// The device operators are assembled on the GPU when the handle first goes
+// there; the host copies of the transforms are built only when asked for
+// (export), and the velocity points with the device transforms when a GPU
+// is present, else with the host ones.
 struct sgdg_vlasov {
     int D = 0, P = 0, k = 0, n = 0;
     SparseIndex ix;
-    std::vector<CSR> Ds;
-    CSR T[4];  // m2n, n2p, p2n, n2m
-    std::vector<double> v_point;  // D x N
+    std::shared_ptr<const DLF1D> dlf;
+    mutable std::unique_ptr<CSR> T[4];    // m2n, n2p, p2n, n2m on the host, built on request
+    mutable std::vector<double> v_point;  // D x N, built on request
+    mutable bool have_vpoint = false;
     std::vector<std::unique_ptr<DeviceCSR>> dDs;
     std::unique_ptr<DeviceCSR> dT[4];
     DevBuf vpt, F, t, s, p, c1, c2, z;
@@ -91,12 +96,55 @@ struct sgdg_vlasov {
     ~sgdg_vlasov() {
         if (stream) cudaStreamDestroy(stream);
     }
+    const CSR& host_transform(int w) const {
+        if (!T[w]) T[w].reset(new CSR(transform_dd(ix, transform_1d(k, n, w))));
+        return *T[w];
+    }
+    // modal coefficients of 2 p_d - 1: 1/sqrt(3) on mode 2 along dimension D + d
+    // of the first block (the tensor product with 1), src/pdes.jl:166-172
+    std::vector<double> v_modal(int d) const {
+        std::vector<double> vm(ix.N, 0.0);
+        vm[(size_t)std::pow((double)k, (double)(D + d))] = 1.0 / std::sqrt(3.0);
+        return vm;
+    }
+    void vpoint_host() const {  // n2p m2n on the host
+        const int64_t N = ix.N;
+        v_point.assign((size_t)D * N, 0.0);
+        std::vector<double> tmp(N), pt(N);
+        auto spmv = [&](const CSR& A, const std::vector<double>& x, std::vector<double>& y) {
+            for (int64_t i = 0; i < A.m; i++) {
+                double acc = 0.0;
+                for (int64_t q = A.rowptr[i]; q < A.rowptr[i + 1]; q++) acc += A.val[q] * x[A.col[q]];
+                y[i] = acc;
+            }
+        };
+        for (int d = 0; d < D; d++) {
+            spmv(host_transform(0), v_modal(d), tmp);
+            spmv(host_transform(1), tmp, pt);
+            std::copy(pt.begin(), pt.end(), v_point.begin() + (size_t)d * N);
+        }
+        have_vpoint = true;
+    }
     void to_gpu() {
         if (stream) return;
         require_gpu();
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        for (auto& A : Ds) dDs.push_back(to_device(A, stream));
-        for (int w = 0; w < 4; w++) dT[w] = to_device(T[w], stream);
+        for (int d = 0; d < P; d++) dDs.push_back(gpu_operator(ix, *dlf, d + 1, stream));
+        for (int w = 0; w < 4; w++) dT[w] = gpu_transform(ix, transform_1d(k, n, w), stream);
+        if (!have_vpoint) {  // n2p m2n with the device transforms
+            const size_t b = sizeof(double) * (size_t)ix.N;
+            DevBuf x(b), y(b), w(b);
+            v_point.assign((size_t)D * ix.N, 0.0);
+            for (int d = 0; d < D; d++) {
+                const std::vector<double> vm = v_modal(d);
+                CK(cudaMemcpyAsync(x.p, vm.data(), b, cudaMemcpyHostToDevice, stream));
+                CK(launch_csr_spmv(dT[0]->d, x.as<double>(), y.as<double>(), stream));
+                CK(launch_csr_spmv(dT[1]->d, y.as<double>(), w.as<double>(), stream));
+                CK(cudaMemcpyAsync(v_point.data() + (size_t)d * ix.N, w.p, b, cudaMemcpyDeviceToHost, stream));
+            }
+            CK(cudaStreamSynchronize(stream));
+            have_vpoint = true;
+        }
         vpt = upload(v_point, stream);
         const size_t b = sizeof(double) * (size_t)ix.N;
         F.alloc(b * D);
@@ -553,6 +601,32 @@ int sgdg_transform_export(int D, int k, int n, int scheme, int which, int64_t* r
     API_END
 }
 
+int sgdg_transform_device_export(int D, int k, int n, int scheme, int which, int64_t* nnz, int64_t* rowptr,
+                                 int32_t* col, double* val) {
+    API_BEGIN
+    NEED(nnz);
+    if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
+    if (k != 2 && k != 3 && k != 5) throw Error(SGDG_EINVAL, "the nodal basis exists for k = 2, 3, 5");
+    require_gpu();
+    const SparseIndex ix = make_index(D, k, n, scheme);
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    std::unique_ptr<DeviceCSR> A;
+    try {
+        A = gpu_transform(ix, transform_1d(k, n, which), st);
+        const CSR h = download_csr(*A, st);
+        *nnz = h.nnz();
+        if (rowptr && col && val) export_csr(h, rowptr, col, val);
+    } catch (...) {
+        A.reset();
+        cudaStreamDestroy(st);
+        throw;
+    }
+    A.reset();
+    cudaStreamDestroy(st);
+    API_END
+}
+
 // ------------------------------------------------------------- Vlasov ----
 int sgdg_vlasov_create(int D, int k, int n, int scheme, sgdg_vlasov** out) {
     API_BEGIN
@@ -565,31 +639,7 @@ int sgdg_vlasov_create(int D, int k, int n, int scheme, sgdg_vlasov** out) {
     v->k = k;
     v->n = n;
     v->ix = make_index(v->P, k, n, scheme);
-    auto dlf = dlf1d(k, n);
-    for (int d = 0; d < v->P; d++) v->Ds.push_back(assemble_dd(v->ix, *dlf, d));
-    for (int w = 0; w < 4; w++) v->T[w] = transform_dd(v->ix, transform_1d(k, n, w));
-    // v_modal_d = tensor product of 1 (coefficient 1 on the first block) and,
-    // along p_d, 2 p_d - 1 (coefficient 1/sqrt(3) on mode 2), src/pdes.jl:166-172
-    const int64_t N = v->ix.N;
-    v->v_point.assign((size_t)D * N, 0.0);
-    std::vector<double> vm(N, 0.0), tmp(N, 0.0);
-    for (int d = 0; d < D; d++) {
-        std::fill(vm.begin(), vm.end(), 0.0);
-        // level (1..1), cell (1..1), mode 1 except mode 2 along dimension D + d
-        vm[(size_t)std::pow((double)k, (double)(D + d))] = 1.0 / std::sqrt(3.0);
-        // m2n then n2p on the host
-        auto spmv = [&](const CSR& A, const std::vector<double>& x, std::vector<double>& y) {
-            for (int64_t i = 0; i < A.m; i++) {
-                double acc = 0.0;
-                for (int64_t q = A.rowptr[i]; q < A.rowptr[i + 1]; q++) acc += A.val[q] * x[A.col[q]];
-                y[i] = acc;
-            }
-        };
-        spmv(v->T[0], vm, tmp);
-        std::vector<double> pt(N);
-        spmv(v->T[1], tmp, pt);
-        std::copy(pt.begin(), pt.end(), v->v_point.begin() + (size_t)d * N);
-    }
+    v->dlf = dlf1d(k, n);
     *out = v.release();
     API_END
 }
@@ -612,6 +662,15 @@ int sgdg_vlasov_v_point(const sgdg_vlasov* v, double* out) {
     API_BEGIN
     NEED(v);
     NEED(out);
+    if (!v->have_vpoint) {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0)
+            const_cast<sgdg_vlasov*>(v)->to_gpu();
+        else {
+            cudaGetLastError();
+            v->vpoint_host();
+        }
+    }
     std::copy(v->v_point.begin(), v->v_point.end(), out);
     API_END
 }
@@ -621,7 +680,7 @@ int sgdg_vlasov_transform_nnz(const sgdg_vlasov* v, int which, int64_t* nnz) {
     NEED(v);
     NEED(nnz);
     if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
-    *nnz = v->T[which].nnz();
+    *nnz = v->host_transform(which).nnz();
     API_END
 }
 
@@ -630,7 +689,7 @@ int sgdg_vlasov_transform_export(const sgdg_vlasov* v, int which, int64_t* rowpt
     NEED(v);
     NEED(rowptr);
     if (which < 0 || which > 3) throw Error(SGDG_EINVAL, "transform must be 0..3 (m2n, n2p, p2n, n2m)");
-    export_csr(v->T[which], rowptr, col, val);
+    export_csr(v->host_transform(which), rowptr, col, val);
     API_END
 }
 

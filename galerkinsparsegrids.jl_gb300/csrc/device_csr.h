@@ -84,6 +84,9 @@ inline std::unique_ptr<DeviceCSR> to_device(const CSR& A, cudaStream_t st) {
 std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st);
 // sum_d s[d] D_d over the union of patterns (the plain advection operator)
 std::unique_ptr<DeviceCSR> gpu_scaled_sum(const SparseIndex& ix, const DLF1D& dlf, const double* s, cudaStream_t st);
+// The D-dim restricted Kronecker product of the 1D transform T1 (the same
+// entries, order and values as transform_dd, nodal.cpp)
+std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, cudaStream_t st);
 // host copy of a device operator
 CSR download_csr(const DeviceCSR& A, cudaStream_t st);
 

@@ -16,6 +16,7 @@
 // holds the same stored entries and the same values as the host one.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 
 #include "../../include/sgdg.h"
@@ -243,7 +244,252 @@ std::unique_ptr<DeviceCSR> merge_terms(const std::vector<const DeviceCSR*>& term
     return R;
 }
 
+// ---------------------------------------------------------- transforms ----
+// The D-dim nodal transforms (src/multidim_nodal_basis.jl:40-109) restricted
+// to the sparse grid: entry (i, j) is prod_d T1[i_d, j_d] (multiplied in
+// dimension order, stopping at an exact 0) over 1D index pairs whose cells
+// nest, for j's level tuple admissible, kept when |value| >= 1e-12 -- the
+// set transform_dd (nodal.cpp) builds column by column.  Here one thread per
+// row i enumerates its columns from the 1D rows of i_d (nesting pairs only,
+// filtered on the host): level tuples, then cell tuples, then mode tuples,
+// each with dimension 0 varying fastest, which is the order of the global
+// index (level blocks in CartesianIndices order, then cells, then modes), so
+// the row comes out sorted.
+constexpr int kTLev = 16;  // levels per dimension (n + 1)
+
+struct TransArgs {
+    int D, k, n, scheme, nlev;
+    int64_t N, kD;
+    const int8_t* levels;
+    const int32_t* lev_off;
+    const int32_t* code2lev;  // (n+1)^D level tuple code -> block, or -1
+    const int64_t* rp1;       // filtered 1D rows
+    const int32_t* col1;
+    const double* val1;
+};
+
+__device__ __forceinline__ void dec1d(int k, int j1, int& L, int& c, int& m) {
+    const int blk = j1 / k;
+    m = j1 - blk * k;                         // 0-based mode
+    L = blk == 0 ? 1 : (32 - __clz(blk)) + 1;  // 1-based level
+    c = L >= 2 ? blk - (1 << (L - 2)) : 0;     // 0-based cell
+}
+
+template <bool FILL>
+__global__ void k_transform(TransArgs A, int32_t* rowlen, const int64_t* __restrict__ rowptr,
+                            int32_t* __restrict__ col, double* __restrict__ val) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const int D = A.D, k = A.k;
+    // (level, cell, mode) of row i per dimension -> its 1D row
+    int lo = 0, hi = A.nlev - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.lev_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const int8_t* Li = A.levels + (size_t)lo * D;
+    int64_t cl = (i - A.lev_off[lo]) / A.kD, ml = (i - A.lev_off[lo]) % A.kD;
+    int a[8], b[8];  // each dimension's 1D row (entry indices; 1D transforms hold < 2^31 entries)
+    for (int d = 0; d < D; d++) {
+        const int L = Li[d];
+        const int64_t nc = (int64_t)1 << (L > 2 ? L - 2 : 0);
+        const int64_t c = cl % nc, m = ml % k;
+        cl /= nc;
+        ml /= k;
+        const int64_t i1 = k * ((L >= 2 ? ((int64_t)1 << (L - 2)) : 0) + c) + m;
+        a[d] = (int)A.rp1[i1];
+        b[d] = (int)A.rp1[i1 + 1];
+    }
+    // level groups of each 1D row: [gs, ge) entries of level gl
+    int ng[8];
+    int gs[8][kTLev], ge[8][kTLev], gl[8][kTLev];
+    for (int d = 0; d < D; d++) {
+        ng[d] = 0;
+        int last = -1;
+        for (int e = a[d]; e < b[d]; e++) {
+            int L, c, m;
+            dec1d(k, A.col1[e], L, c, m);
+            if (L != last) {
+                gs[d][ng[d]] = e;
+                gl[d][ng[d]] = L;
+                if (ng[d] > 0) ge[d][ng[d] - 1] = e;
+                ng[d]++;
+                last = L;
+            }
+        }
+        if (ng[d] == 0) {  // an empty 1D row: no entries in row i
+            if (!FILL) rowlen[i] = 0;
+            return;
+        }
+        ge[d][ng[d] - 1] = b[d];
+    }
+    int64_t w = FILL ? rowptr[i] : 0;
+    int32_t cnt = 0;
+    int g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (;;) {  // level tuples, dimension 0 fastest
+        int code = 0, lsum = 0, mult = 1;
+        for (int d = 0; d < D; d++) {
+            code += (gl[d][g[d]] - 1) * mult;
+            mult *= A.n + 1;
+            lsum += gl[d][g[d]];
+        }
+        const int blk = (A.scheme == 0 && lsum > A.n + D) ? -1 : A.code2lev[code];
+        if (blk >= 0) {
+            const int64_t base = A.lev_off[blk];
+            // cell tuples within the groups: cs = first entry of the cell group, ce its end
+            int cs[8], ce[8];
+            for (int d = 0; d < D; d++) {
+                cs[d] = gs[d][g[d]];
+                ce[d] = cs[d];
+                int L0, c0, m0;
+                dec1d(k, A.col1[cs[d]], L0, c0, m0);
+                while (ce[d] < ge[d][g[d]]) {
+                    int L, c, m;
+                    dec1d(k, A.col1[ce[d]], L, c, m);
+                    if (c != c0) break;
+                    ce[d]++;
+                }
+            }
+            for (;;) {
+                int64_t cell_lin = 0, cstride = 1;
+                for (int d = 0; d < D; d++) {
+                    int L, c, m;
+                    dec1d(k, A.col1[cs[d]], L, c, m);
+                    cell_lin += (int64_t)c * cstride;
+                    cstride <<= (L > 2 ? L - 2 : 0);
+                }
+                // mode tuples within the cell groups
+                int e[8];
+                for (int d = 0; d < D; d++) e[d] = cs[d];
+                for (;;) {
+                    double v = 1.0;
+                    for (int d = 0; d < D; d++) {
+                        v = __dmul_rn(v, A.val1[e[d]]);
+                        if (v == 0.0) break;
+                    }
+                    if (!(fabs(v) < 1e-12)) {
+                        if (FILL) {
+                            int64_t mode_lin = 0, ms = 1;
+                            for (int d = 0; d < D; d++) {
+                                int L, c, m;
+                                dec1d(k, A.col1[e[d]], L, c, m);
+                                mode_lin += m * ms;
+                                ms *= k;
+                            }
+                            col[w] = (int32_t)(base + A.kD * cell_lin + mode_lin);
+                            val[w] = v;
+                            w++;
+                        }
+                        cnt++;
+                    }
+                    int d = 0;
+                    for (; d < D; d++) {  // next mode tuple
+                        if (++e[d] < ce[d]) break;
+                        e[d] = cs[d];
+                    }
+                    if (d == D) break;
+                }
+                int d = 0;
+                for (; d < D; d++) {  // next cell tuple
+                    if (ce[d] < ge[d][g[d]]) {
+                        cs[d] = ce[d];
+                        int L0, c0, m0;
+                        dec1d(k, A.col1[cs[d]], L0, c0, m0);
+                        while (ce[d] < ge[d][g[d]]) {
+                            int L, c, m;
+                            dec1d(k, A.col1[ce[d]], L, c, m);
+                            if (c != c0) break;
+                            ce[d]++;
+                        }
+                        break;
+                    }
+                    cs[d] = gs[d][g[d]];  // wrap to the first cell group of the level
+                    ce[d] = cs[d];
+                    int L0, c0, m0;
+                    dec1d(k, A.col1[cs[d]], L0, c0, m0);
+                    while (ce[d] < ge[d][g[d]]) {
+                        int L, c, m;
+                        dec1d(k, A.col1[ce[d]], L, c, m);
+                        if (c != c0) break;
+                        ce[d]++;
+                    }
+                }
+                if (d == D) break;
+            }
+        }
+        int d = 0;
+        for (; d < D; d++) {  // next level tuple
+            if (++g[d] < ng[d]) break;
+            g[d] = 0;
+        }
+        if (d == D) break;
+    }
+    if (!FILL) rowlen[i] = cnt;
+}
+
 }  // namespace
+
+std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, cudaStream_t st) {
+    require_gpu();
+    const int D = ix.D, k = ix.k, n = ix.n;
+    if (n + 1 > kTLev) throw Error(SGDG_EUNSUPPORTED, "more than 16 levels per dimension");
+    // 1D rows restricted to the index pairs whose cells nest (relevant_cell_1D)
+    // support [c w, (c + 1) w) of the 1D index j1 (level L, 0-based cell c),
+    // computed as transform_dd's nesting test computes it
+    auto cellrange = [&](int j1, double& lo, double& hi) {
+        const int blk = j1 / k;
+        int L = 1;
+        while (L < 32 && (blk >> (L - 1)) != 0) L++;
+        const int c = L >= 2 ? blk - (1 << (L - 2)) : 0;
+        const double w = 1.0 / (double)ncells(L);
+        lo = c * w;
+        hi = (c + 1) * w;
+    };
+    std::vector<int64_t> rp(T1.m + 1, 0);
+    std::vector<int32_t> cl;
+    std::vector<double> vl;
+    std::vector<std::pair<int32_t, double>> row;
+    for (int64_t r = 0; r < T1.m; r++) {
+        double a1, b1;
+        cellrange((int)r, a1, b1);
+        row.clear();
+        for (int64_t p = T1.rowptr[r]; p < T1.rowptr[r + 1]; p++) {
+            double a2, b2;
+            cellrange(T1.col[p], a2, b2);
+            if ((a1 <= a2 && b1 >= b2) || (a1 >= a2 && b1 <= b2)) row.push_back({T1.col[p], T1.val[p]});
+        }
+        // the enumeration walks each row by level, cell and mode: columns ascending
+        std::sort(row.begin(), row.end(), [](const std::pair<int32_t, double>& x, const std::pair<int32_t, double>& y) {
+            return x.first < y.first;
+        });
+        for (auto& e : row) {
+            cl.push_back(e.first);
+            vl.push_back(e.second);
+        }
+        rp[r + 1] = (int64_t)cl.size();
+    }
+    std::vector<int8_t> lv(ix.levels.size());
+    for (size_t q = 0; q < lv.size(); q++) lv[q] = (int8_t)ix.levels[q];
+    std::vector<int32_t> lo(ix.lev_off.begin(), ix.lev_off.end());
+    DevBuf d_lv = upload(lv, st), d_lo = upload(lo, st), d_code = upload(ix.code2lev, st), d_rp = upload(rp, st),
+           d_cl = upload(cl, st), d_vl = upload(vl, st);
+    TransArgs A{D, k, n, ix.scheme, ix.nlev, ix.N, ix.kD, d_lv.as<int8_t>(), d_lo.as<int32_t>(), d_code.as<int32_t>(),
+                d_rp.as<int64_t>(), d_cl.as<int32_t>(), d_vl.as<double>()};
+    DevBuf rowlen(sizeof(int32_t) * (size_t)ix.N);
+    k_transform<false><<<grid_for(ix.N), 256, 0, st>>>(A, rowlen.as<int32_t>(), nullptr, nullptr, nullptr);
+    CK(cudaGetLastError());
+    std::vector<int64_t> rph = scan_rows(rowlen, ix.N, st);
+    auto R = std::make_unique<DeviceCSR>();
+    R->rowptr = upload(rph, st);
+    R->col.alloc(sizeof(int32_t) * (size_t)rph[ix.N]);
+    R->val.alloc(sizeof(double) * (size_t)rph[ix.N]);
+    k_transform<true><<<grid_for(ix.N), 256, 0, st>>>(A, nullptr, R->rowptr.as<int64_t>(), R->col.as<int32_t>(),
+                                                      R->val.as<double>());
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    finish_device_csr(*R, rph, ix.N, st);
+    return R;
+}
 
 std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st) {
     require_gpu();

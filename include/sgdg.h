@@ -135,6 +135,11 @@ int sgdg_transform_1d_export(int k, int n, int which, int64_t *rowptr, int32_t *
  * tensored over D dimensions on the sparse grid, CSR (N x N). */
 int sgdg_transform_nnz(int D, int k, int n, int scheme, int which, int64_t *nnz);
 int sgdg_transform_export(int D, int k, int n, int scheme, int which, int64_t *rowptr, int32_t *col, double *val);
+/* The same transform assembled on the GPU (the handle of the Vlasov evolver
+ * builds its device transforms this way): the same entries, order and values.
+ * Writes *nnz; with rowptr, col and val all non-NULL also the CSR. */
+int sgdg_transform_device_export(int D, int k, int n, int scheme, int which, int64_t *nnz, int64_t *rowptr,
+                                 int32_t *col, double *val);
 
 /* vlasov_evolve (src/pdes.jl:131-227) for D space dimensions: phase space of
  * 2D dimensions ordered x_1..x_D, p_1..p_D, velocity v_d = 2 p_d - 1.  The

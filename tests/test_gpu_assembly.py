@@ -38,3 +38,16 @@ def test_plain_advection_uses_the_same_operator(sgdg, O):
     _, st = sgdg.advect_evolve(D, k, n, a, f0, 0.0, steps * dt, nsteps=steps, method="plain")
     ref = O.CSR(O.advection_matrix_raw(D, k, n, a)).rk4(f0, dt, steps, nthreads=1)
     assert np.linalg.norm(st[-1] - ref) <= 1e-10 * np.linalg.norm(ref)  # FP64 SpMV with FMA on the GPU
+
+
+WHICH = [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"), ("nodal", "modal")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,k,n,scheme", [(2, 2, 3, "sparse"), (2, 3, 4, "sparse"), (3, 2, 3, "sparse"),
+                                          (4, 2, 3, "sparse"), (2, 5, 3, "sparse"), (2, 2, 3, "full")])
+def test_device_transforms_equal_host(sgdg, D, k, n, scheme):
+    # the restricted Kronecker products (src/multidim_nodal_basis.jl:40-109)
+    for w in WHICH:
+        assert same_bits(sgdg.transform(D, k, n, *w, scheme=scheme, device=True),
+                         sgdg.transform(D, k, n, *w, scheme=scheme)), w
