@@ -40,8 +40,13 @@ enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1, MF_KIND_VLASOV = 2 };
 // TILE_RK: the pass completes the right-hand side and applies the RK4 update;
 // TILE_STORE: the result goes to a scratch vector; TILE_WACC: times a point
 // weight, added into the point-basis accumulator; TILE_WAIT_IN: the input
-// was written by the previous phase of this launch (wait before gathering).
-enum : int { TILE_FIRST = 1, TILE_LAST = 2, TILE_RK = 4, TILE_STORE = 8, TILE_WACC = 16, TILE_WAIT_IN = 32 };
+// was written by the previous phase of this launch (wait before gathering);
+// TILE_SUMIN: the input is the sum of the D scratch vectors src, src + 2, ...
+// (the per-dimension point products of the Vlasov right-hand side), added in
+// that order.
+enum : int {
+    TILE_FIRST = 1, TILE_LAST = 2, TILE_RK = 4, TILE_STORE = 8, TILE_WACC = 16, TILE_WAIT_IN = 32, TILE_SUMIN = 64
+};
 enum : int { TABLE_DERIVATIVE = -1 };  // MFItem::tab; 0..3: the nodal transforms
 
 struct MFClass {
@@ -65,7 +70,8 @@ struct MFClass {
     const int32_t* t_rowptr[4];
     const int32_t* t_ent[4];
     const float* t_val[4];
-    float* vb[3];             // per slot N: two ping-pong vectors and the point-basis accumulator
+    float* vbase;             // scratch vector v of slot s at vbase + v vstride + s N (2 per phase dimension)
+    int64_t vstride;
     const float* vw;          // per slot 2 x D x N: weight of term d at [d N] (hi) and [(D + d) N] (lo)
 };
 

@@ -247,7 +247,8 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         cp_async_wait_all();
     } else {
         // a scratch vector written in this launch by other SMs: L2 loads (.cg)
-        const float* __restrict__ vin = C.vb[it.src];
+        const float* __restrict__ vin = C.vbase + (size_t)it.src * C.vstride;
+        const int nsum = (it.flags & TILE_SUMIN) ? C.D : 1;
         tile_columns(W, lw, [&](int j, int r0, int rstep) {
             float* xc = X + j;
             const int s = cslot[j];
@@ -257,9 +258,13 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             }
             const float* base = vin + (size_t)s * C.N + ca[j];
             const int bj = cb[j];
+            const size_t step2 = 2 * (size_t)C.vstride;
             for (int row = r0; row < m; row += rstep) {
                 const int2 ri = rinfo[row];
-                xc[row * W] = __ldcg(base + ri.x + (bj << ri.y));
+                const float* p = base + ri.x + (bj << ri.y);
+                float v = __ldcg(p);
+                for (int q = 1; q < nsum; q++) v += __ldcg(p + q * step2);  // the D products, in order
+                xc[row * W] = v;
             }
         });
     }
@@ -301,7 +306,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     if (it.flags & (TILE_STORE | TILE_WACC)) {
         // Vlasov: a transform's result to a scratch vector, or the point
         // product w_d .* result added into the point-basis accumulator
-        float* __restrict__ out = C.vb[it.dst];
+        float* __restrict__ out = C.vbase + (size_t)it.dst * C.vstride;
         const bool wacc = (it.flags & TILE_WACC) != 0;
         tile_columns(W, lw, [&](int j, int r0, int rstep) {
             const int s = cslot[j];

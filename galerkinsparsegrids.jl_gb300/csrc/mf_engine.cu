@@ -92,8 +92,8 @@ int MFEngine::add(const SolveSpec& sp, const double* y0, const float* weights) {
 
 int64_t MFEngine::solve_bytes(int64_t N, int64_t Ns, int kind, int D) {
     // y, acc (FP64), two stage inputs (FP32), partial sums (FP32); Vlasov:
-    // three scratch vectors and 2 D point weights (FP32)
-    return Ns * (8 + 8 + 4 + 4) + N * 4 + (kind == MF_KIND_VLASOV ? N * 4 * (3 + 2 * (int64_t)D) : 0);
+    // two scratch vectors per phase dimension and 2 D point weights (FP32)
+    return Ns * (8 + 8 + 4 + 4) + N * 4 + (kind == MF_KIND_VLASOV ? N * 4 * (4 * (int64_t)D) : 0);
 }
 
 int64_t MFEngine::dead_bytes() const {
@@ -249,7 +249,7 @@ void MFEngine::plan() {
         c.rhs.alloc(sizeof(float) * ns * c.N);
         const bool vlasov = s0.spec.kind == MF_KIND_VLASOV;
         if (vlasov) {
-            c.vb.alloc(sizeof(float) * 3 * ns * c.N);
+            c.vb.alloc(sizeof(float) * 2 * (size_t)D * ns * c.N);  // two ping-pong vectors per phase dimension
             c.vw.alloc(sizeof(float) * 2 * (size_t)D * ns * c.N);
             for (int sl = 0; sl < ns; sl++) {
                 const Solve& s = solves_[c.slots[sl]];
@@ -347,7 +347,8 @@ void MFEngine::plan() {
                 m.t_ent[w] = T.t[w].ent.as<int32_t>();
                 m.t_val[w] = T.t[w].val.as<float>();
             }
-            for (int b = 0; b < 3; b++) m.vb[b] = c.vb.as<float>() + (size_t)b * c.slots.size() * c.N;
+            m.vbase = c.vb.as<float>();
+            m.vstride = (int64_t)c.slots.size() * c.N;
             m.vw = c.vw.as<float>();
         }
         ch.push_back(m);
@@ -381,8 +382,14 @@ void MFEngine::plan() {
 void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only,
                            const std::map<std::pair<int, int>, MFTile>* shapes, int chunk, int nchunks,
                            std::vector<std::array<int, 3>>* ranges) {
+    struct Phase {
+        std::vector<MFItem> items;
+        int depth = 0;      // longest chain of phases before it in the group
+        int done_key = 0;   // counter it increments (phases of a join share one)
+        int wait_key = -1;  // counter it waits for (-1: none)
+    };
     struct Group {
-        std::vector<std::vector<MFItem>> phases;
+        std::vector<Phase> phases;
     };
     std::vector<Group> groups;
     size_t smem = 64;
@@ -414,7 +421,8 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
             if (ranges) ranges->push_back({(int)ci, s0, s1 - s0});
             Group grp;
             // one phase: tiles of every pencil along d over the group's slots
-            auto phase = [&](int d, int tab, int src, int dst, int flags, int wsel) {
+            auto phase = [&](int d, int tab, int src, int dst, int flags, int wsel, int depth, int done_key,
+                             int wait_key) {
                 int kd1 = 1;
                 for (int q = 0; q < d; q++) kd1 *= k;
                 std::vector<MFItem> list;
@@ -449,7 +457,12 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                         list.push_back(it);
                     }
                 }
-                grp.phases.push_back(std::move(list));
+                Phase ph;
+                ph.items = std::move(list);
+                ph.depth = depth;
+                ph.done_key = done_key;
+                ph.wait_key = wait_key;
+                grp.phases.push_back(std::move(ph));
             };
             // the RK state is never updated while tuning (no state changes)
             const int rk = !sp.apply && !pass_only ? TILE_RK : 0;
@@ -457,61 +470,86 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                 // one pass per dimension accumulating into rhs; the last applies the RK update
                 for (size_t ph = 0; ph < dims.size(); ph++) {
                     const bool last = ph + 1 == dims.size();
-                    phase(dims[ph], TABLE_DERIVATIVE, -1, 0,
-                          (ph == 0 ? TILE_FIRST : 0) | (last ? TILE_LAST | rk : 0), 0);
+                    phase(dims[ph], TABLE_DERIVATIVE, -1, 0, (ph == 0 ? TILE_FIRST : 0) | (last ? TILE_LAST | rk : 0),
+                          0, (int)ph, (int)ph, (int)ph - 1);
                 }
             } else {
                 // Vlasov right-hand side (src/pdes.jl:174-192) as sweeps: for each
-                // phase dimension d, D_d then the modal->nodal and nodal->points
-                // transforms (one sweep per dimension each; the restricted
-                // Kronecker products factor exactly because the 1D maps are
-                // level-triangular), times the point weight of d into the
-                // accumulator; then points->nodal and nodal->modal, whose last
-                // sweep applies the RK update.  Every phase after the first reads
-                // what the previous phase wrote.
-                const int P = D, A = 0, ACC = 2;
+                // phase dimension d a chain -- D_d, then the modal->nodal and
+                // nodal->points transforms (one sweep per dimension each; the
+                // restricted Kronecker products factor exactly because the 1D
+                // maps are level-triangular), the last sweep times the point
+                // weight of d -- in its own two scratch vectors (2d, 2d + 1), so
+                // the D chains run concurrently; then points->nodal, whose
+                // first sweep gathers the sum of the D products (in order d =
+                // 0, 1, ...) once every chain is done, and nodal->modal, whose
+                // last sweep applies the RK update.  Within a chain every sweep
+                // reads what the previous one wrote.
+                const int P = D, kJoin = 1 << 20;
+                int key = 0, maxdepth = 0, prod = -1;
                 for (int d = 0; d < P; d++) {
-                    phase(d, TABLE_DERIVATIVE, -1, A, TILE_STORE | (d > 0 ? TILE_WAIT_IN : 0), 0);
-                    int cur = A;
+                    int depth = 0, prev = -1, cur = 2 * d;
+                    auto link = [&](int q, int tab, int src, int dst, int flags, int wsel, int done) {
+                        phase(q, tab, src, dst, flags | (prev >= 0 ? TILE_WAIT_IN : 0), wsel, depth, done, prev);
+                        prev = done;
+                        depth++;
+                    };
+                    link(d, TABLE_DERIVATIVE, -1, cur, TILE_STORE, 0, key++);
                     for (int q = 0; q < P; q++, cur ^= 1)
-                        phase(q, TRANSFORM_MODAL_TO_NODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
+                        link(q, TRANSFORM_MODAL_TO_NODAL, cur, cur ^ 1, TILE_STORE, 0, key++);
                     for (int q = 0; q < P - 1; q++, cur ^= 1)
-                        phase(q, TRANSFORM_NODAL_TO_POINTS, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
-                    phase(P - 1, TRANSFORM_NODAL_TO_POINTS, cur, ACC,
-                          TILE_WACC | TILE_WAIT_IN | (d == 0 ? TILE_FIRST : 0), d);
+                        link(q, TRANSFORM_NODAL_TO_POINTS, cur, cur ^ 1, TILE_STORE, 0, key++);
+                    link(P - 1, TRANSFORM_NODAL_TO_POINTS, cur, cur ^ 1, TILE_WACC | TILE_FIRST, d, kJoin);
+                    prod = (cur ^ 1) - 2 * d;  // parity of the product vectors (the same for every chain)
+                    maxdepth = std::max(maxdepth, depth);
                 }
-                phase(0, TRANSFORM_POINTS_TO_NODAL, ACC, A, TILE_STORE | TILE_WAIT_IN, 0);
-                int cur = A;
-                for (int q = 1; q < P; q++, cur ^= 1)
-                    phase(q, TRANSFORM_POINTS_TO_NODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
-                for (int q = 0; q < P - 1; q++, cur ^= 1)
-                    phase(q, TRANSFORM_NODAL_TO_MODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0);
-                phase(P - 1, TRANSFORM_NODAL_TO_MODAL, cur, 0, TILE_FIRST | TILE_LAST | rk | TILE_WAIT_IN, 0);
+                int depth = maxdepth, prev = kJoin, cur = prod ^ 1;  // a vector holding no product
+                phase(0, TRANSFORM_POINTS_TO_NODAL, prod, cur, TILE_STORE | TILE_WAIT_IN | TILE_SUMIN, 0, depth++, key,
+                      prev);
+                prev = key++;
+                for (int q = 1; q < P; q++, cur ^= 1) {
+                    phase(q, TRANSFORM_POINTS_TO_NODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0, depth++, key, prev);
+                    prev = key++;
+                }
+                for (int q = 0; q < P - 1; q++, cur ^= 1) {
+                    phase(q, TRANSFORM_NODAL_TO_MODAL, cur, cur ^ 1, TILE_STORE | TILE_WAIT_IN, 0, depth++, key, prev);
+                    prev = key++;
+                }
+                phase(P - 1, TRANSFORM_NODAL_TO_MODAL, cur, 0, TILE_FIRST | TILE_LAST | rk | TILE_WAIT_IN, 0, depth++, key,
+                      prev);
             }
             groups.push_back(std::move(grp));
         }
     }
-    // counters: 0 hands out items; one per (group, phase)
+    // counters: 0 hands out items; one per (group, done key).  A phase waits
+    // for every item of the phases that increment its wait key.
     nctr = 1;
-    std::vector<std::vector<int>> ctr_of(groups.size());
+    std::vector<std::map<int, int>> ctr_of(groups.size());
+    std::vector<std::map<int, int>> items_of(groups.size());
     for (size_t g = 0; g < groups.size(); g++)
-        for (size_t p = 0; p < groups[g].phases.size(); p++) ctr_of[g].push_back(nctr++);
-    // wavefront order: phase p of group g in step g + kWaveLag p, older groups
-    // first within a step, so a phase's predecessor was handed out kWaveLag
-    // steps earlier (about kWaveLag x phases-per-step items before it)
-    size_t pmax = 0;
-    for (auto& g : groups) pmax = std::max(pmax, g.phases.size());
-    const size_t G = groups.size();
+        for (const Phase& ph : groups[g].phases) {
+            if (!ctr_of[g].count(ph.done_key)) ctr_of[g][ph.done_key] = nctr++;
+            items_of[g][ph.done_key] += (int)ph.items.size();
+        }
+    // wavefront order: a phase of depth p of group g in step g + kWaveLag p,
+    // deeper phases (older groups) first within a step, so a phase's
+    // predecessors were handed out at least kWaveLag steps earlier
+    int dmax = 0;
+    for (auto& g : groups)
+        for (const Phase& ph : g.phases) dmax = std::max(dmax, ph.depth);
+    const size_t G = groups.size(), pmax = (size_t)dmax + 1;
     for (size_t t = 0; t < G + kWaveLag * pmax; t++)
         for (size_t pp = pmax; pp-- > 0;) {
             if (t < kWaveLag * pp || t - kWaveLag * pp >= G) continue;
-            const size_t g = t - kWaveLag * pp, p = pp;
-            if (p >= groups[g].phases.size()) continue;
-            for (MFItem it : groups[g].phases[p]) {
-                it.done_ctr = ctr_of[g][p];
-                it.wait_ctr = p > 0 ? ctr_of[g][p - 1] : -1;
-                it.wait_need = p > 0 ? (int32_t)groups[g].phases[p - 1].size() : 0;
-                items.push_back(it);
+            const size_t g = t - kWaveLag * pp;
+            for (const Phase& ph : groups[g].phases) {
+                if (ph.depth != (int)pp) continue;
+                for (MFItem it : ph.items) {
+                    it.done_ctr = ctr_of[g].at(ph.done_key);
+                    it.wait_ctr = ph.wait_key >= 0 ? ctr_of[g].at(ph.wait_key) : -1;
+                    it.wait_need = ph.wait_key >= 0 ? items_of[g].at(ph.wait_key) : 0;
+                    items.push_back(it);
+                }
             }
         }
     int tb = 0;

@@ -95,7 +95,7 @@ class MFEngine {
         int64_t N = 0, Ns = 0;
         std::vector<int> slots;                    // solve id per slot
         DevBuf y, acc, u0, u1, rhs, dt, coef, status, blockoff;
-        DevBuf vb, vw;  // Vlasov: 3 scratch vectors per slot, point weights per slot
+        DevBuf vb, vw;  // Vlasov: 2 scratch vectors per phase dimension and slot, point weights per slot
     };
 
     void plan();
