@@ -445,12 +445,15 @@ __global__ void __launch_bounds__(kMFThreads, 3)
     __shared__ MFItem s_it;
     __shared__ MFClass s_cls;
     __shared__ int s_cls_id;   // class in s_cls (-1: none)
-    __shared__ int s_cached;   // class whose table is in shared memory (-1: none)
+    __shared__ const int32_t* s_cached;  // the table in shared memory, by its global row pointers (null: none)
     const int tid = threadIdx.x;
     constexpr int kItemWords = sizeof(MFItem) / 4;
     constexpr int kClsWords = sizeof(MFClass) / 4;
     static_assert(kItemWords <= 32, "item fits one warp");
-    if (tid == 0) s_cls_id = s_cached = -1;
+    if (tid == 0) {
+        s_cls_id = -1;
+        s_cached = nullptr;
+    }
     if (tid == 32) s_item = atomicAdd(ctr, 1);
     int done = -1;  // thread 0: completion counter of the last finished item
     for (;;) {
@@ -492,13 +495,13 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             int* trow = reinterpret_cast<int*>(smem);
             int* tent = trow + C.s_nrow;
             float* tval = smem + (((C.s_nrow + C.s_nent) * 4 + 15) / 16) * 4;
-            if (s_cached != it.cls) {  // copy the class's operator table (uniform branch)
+            if (s_cached != C.s_rowptr) {  // copy the operator table (uniform branch; classes of one (k, n) share it)
                 for (int i = tid; i < C.s_nrow; i += kMFThreads) trow[i] = C.s_rowptr[i];
                 for (int i = tid; i < C.s_nent; i += kMFThreads) tent[i] = C.s_ent[i];
                 for (int i = tid; i < C.s_nval / 4; i += kMFThreads)
                     reinterpret_cast<float4*>(tval)[i] = reinterpret_cast<const float4*>(C.s_val)[i];
                 __syncthreads();
-                if (tid == 0) s_cached = it.cls;
+                if (tid == 0) s_cached = C.s_rowptr;
             }
             T = OpTable{trow, tent, tval};
         }
