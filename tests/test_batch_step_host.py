@@ -43,3 +43,19 @@ def test_step_host_equals_upload_step_download(sgdg, chunks):
     assert np.array_equal(y2, ref)
     b.close()
     b2.close()
+
+
+@pytest.mark.gpu
+def test_step_host_on_an_empty_batch(sgdg):
+    b = sgdg.Batch()
+    y = np.zeros(0)
+    b.step_host(y.ctypes.data, y.ctypes.data, nsteps=2, chunks=4)  # nothing to move or step
+    b.close()
+
+
+@pytest.mark.gpu
+def test_step_host_rejects_a_wrong_size(sgdg):
+    b = sgdg.Batch()
+    with pytest.raises(ValueError):
+        b.step_host(np.zeros(3), nsteps=1)
+    b.close()

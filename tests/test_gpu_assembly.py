@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 CASES = [(1, 3, 5, "sparse"), (2, 3, 4, "sparse"), (3, 2, 3, "sparse"), (2, 2, 3, "full"), (4, 2, 3, "sparse"),
-         (3, 3, 3, "sparse"), (2, 5, 3, "sparse")]
+         (3, 3, 3, "sparse"), (2, 5, 3, "sparse"), (3, 2, 2, "full")]
 
 
 def same_bits(A, B):
@@ -44,8 +44,9 @@ WHICH = [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"), ("nodal",
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("D,k,n,scheme", [(2, 2, 3, "sparse"), (2, 3, 4, "sparse"), (3, 2, 3, "sparse"),
-                                          (4, 2, 3, "sparse"), (2, 5, 3, "sparse"), (2, 2, 3, "full")])
+@pytest.mark.parametrize("D,k,n,scheme", [(1, 3, 4, "sparse"), (2, 2, 3, "sparse"), (2, 3, 4, "sparse"),
+                                          (3, 2, 3, "sparse"), (4, 2, 3, "sparse"), (2, 5, 3, "sparse"),
+                                          (2, 2, 3, "full")])
 def test_device_transforms_equal_host(sgdg, D, k, n, scheme):
     # the restricted Kronecker products (src/multidim_nodal_basis.jl:40-109)
     for w in WHICH:
