@@ -404,6 +404,40 @@ def advect_evolve(D, k, n, a, f0, time0, time1, order="rk4", scheme="sparse", dt
     return times, list(states)
 
 
+def norm_squared(coeffs, basis="hier"):
+    """Sum of the squared coefficients (src/pdes.jl:228-235): the L2 norm
+    squared in an orthonormal basis ("hier" or "pos")."""
+    if basis not in ("hier", "pos"):
+        raise NotImplementedError("nodal and point basis norms are not implemented (as in the reference)")
+    c = np.asarray(coeffs, np.float64)
+    return float(np.dot(c, c))
+
+
+def wave_evolve_1D(k, max_level, f0, v0, time0, time1, basis="hier", order="rk4", dt=None, nsteps=None, nout=2,
+                   method="plain"):
+    """wave_evolve_1D (src/pdes.jl:89-130) in the hierarchical basis, where
+    the 1D sparse grid is the full grid and the evolution is wave_evolve(1, ...)."""
+    if basis != "hier":
+        raise ValueError("basis: only \"hier\" is implemented on the GPU")
+    return wave_evolve(1, k, max_level, f0, v0, time0, time1, order=order, dt=dt, nsteps=nsteps, nout=nout,
+                       method=method)
+
+
+def energy_func_1D(k, level, soln, basis="hier"):
+    """||D u||^2 + ||u_t||^2 per stored state of a 1D solution
+    (src/pdes.jl:237-255), D the periodic hierarchical 1D operator."""
+    if basis != "hier":
+        raise ValueError("basis: only \"hier\" is implemented")
+    D_op = periodic_DLF_matrix(k, level)
+    times, states = soln
+    energies = []
+    for st in states:
+        st = np.asarray(st, np.float64)
+        h = int(round(st.size / 2))
+        energies.append(norm_squared(D_op @ st[:h]) + norm_squared(st[h:]))
+    return np.array(times), np.array(energies)
+
+
 def energy_func(D, k, n, soln, scheme="sparse", op=None):
     """sum_d ||D_d u||^2 + ||u_t||^2 per stored state (src/pdes.jl:258-273), D_d applied on the GPU."""
     op = op or SparseGridOperator(D, k, n, scheme)

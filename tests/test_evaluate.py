@@ -2,7 +2,9 @@
 Monte Carlo error measures (src/error_measure.jl:12-45): the host logic on
 CPU; on the GPU the batched FP64 evaluator against the oracle's restatement
 (or_reconstruct) at random, boundary and midpoint coordinates, against the
-basis products for unit coefficient vectors, and the argument errors."""
+basis products for unit coefficient vectors, and the argument errors; the
+energy functions of src/pdes.jl:228-273 against a direct computation and the
+reference's 1D energy known answer (test/solvers.jl:34-41)."""
 import numpy as np
 import pytest
 
@@ -122,3 +124,32 @@ def test_points_outside_the_domain(sgdg, O):
         assert e.value.code == 1
     # an empty batch is a no-op
     assert sgdg.reconstruct_DG(D, k, n, c, np.zeros((0, D))).shape == (0,)
+
+
+# ------------------------------------------------- energies (pdes.jl) ----
+def test_norm_squared_and_energy_1d_host(sgdg, O):
+    assert sgdg.norm_squared([3.0, 4.0]) == 25.0
+    with pytest.raises(NotImplementedError):
+        sgdg.norm_squared([1.0], basis="nodal")
+    k, level = 3, 4
+    rng = np.random.default_rng(8)
+    n1 = k << level
+    states = [rng.standard_normal(2 * n1) for _ in range(3)]
+    times, E = sgdg.energy_func_1D(k, level, (np.array([0.0, 0.5, 1.0]), states))
+    D = O.periodic_DLF_matrix(k, level)
+    for s, e in zip(states, E):
+        want = np.sum((D @ s[:n1]) ** 2) + np.sum(s[n1:] ** 2)
+        assert abs(e - want) <= 1e-12 * want
+    with pytest.raises(ValueError):
+        sgdg.energy_func_1D(k, level, (times, states), basis="pos")
+
+
+@pytest.mark.gpu
+def test_wave_1d_energy_known_answer(sgdg):
+    # test/solvers.jl:34-41: k = 4, level = 4, u = sin(2 pi x), u_t = 2 pi cos(2 pi x):
+    # sqrt(energy) = 2 pi to 1e-7 at every stored time
+    f0 = lambda x: np.sin(2 * np.pi * x[:, 0])
+    v0 = lambda x: 2 * np.pi * np.cos(2 * np.pi * x[:, 0])
+    soln = sgdg.wave_evolve_1D(4, 4, f0, v0, 0.0, 1.0, nsteps=2000, nout=5)
+    _, E = sgdg.energy_func_1D(4, 4, soln)
+    assert np.max(np.abs(np.sqrt(E) - 2 * np.pi)) < 1e-7
