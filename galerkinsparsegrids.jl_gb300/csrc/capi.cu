@@ -22,8 +22,10 @@ namespace sgdg {
 cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st);
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
                            int stage, cudaStream_t st);
-cudaError_t launch_vlasov_combine(const double* w, const double* p, const double* acc_in, const double* other,
-                                  double* out, int64_t n, cudaStream_t st);
+cudaError_t launch_csr_spmv_multi(const DevCSR& A, int nv, const double* x, int64_t xi, int64_t xs, double* y,
+                                  int64_t yi, int64_t ys, cudaStream_t st);
+cudaError_t launch_vlasov_points(const double* v, const double* F, const double* pt, int D, int64_t n, double* out,
+                                 cudaStream_t st);
 cudaError_t launch_wait_selftest(const int* ctr, int need, int* err, cudaStream_t st);
 
 static thread_local std::string g_err;
@@ -91,7 +93,7 @@ struct sgdg_vlasov {
     mutable bool have_vpoint = false;
     std::vector<std::unique_ptr<DeviceCSR>> dDs;
     std::unique_ptr<DeviceCSR> dT[4];
-    DevBuf vpt, F, t, s, p, c1, c2, z;
+    DevBuf vpt, F, t, s, p, c, z;  // t, s, p: P vectors each, interleaved (t[i * P + d])
     cudaStream_t stream = nullptr;
     ~sgdg_vlasov() {
         if (stream) cudaStreamDestroy(stream);
@@ -148,34 +150,26 @@ struct sgdg_vlasov {
         vpt = upload(v_point, stream);
         const size_t b = sizeof(double) * (size_t)ix.N;
         F.alloc(b * D);
-        t.alloc(b);
-        s.alloc(b);
-        p.alloc(b);
-        c1.alloc(b);
-        c2.alloc(b);
+        t.alloc(b * P);
+        s.alloc(b * P);
+        p.alloc(b * P);
+        c.alloc(b);
         z.alloc(b);
     }
-    // z = p2n (-sum_d v_d .* n2p m2n Dx_d u + sum_d F_d .* n2p m2n Dp_d u)
+    // z = p2n (-sum_d v_d .* n2p m2n Dx_d u + sum_d F_d .* n2p m2n Dp_d u):
+    // the P derivatives, interleaved (the P values of one coefficient share a
+    // sector), then each transform on all P of them in one pass over its
+    // matrix, the point products, and p2n
     cudaError_t rhs_points(const double* u) {
         const int64_t N = ix.N;
-        const double* vp = vpt.as<double>();
-        const double* Fp = F.as<double>();
         double *tt = t.as<double>(), *ss = s.as<double>(), *pp = p.as<double>();
-        double *a1 = c1.as<double>(), *a2 = c2.as<double>(), *zz = z.as<double>();
         cudaError_t e = cudaSuccess;
-        for (int d = 0; d < P && e == cudaSuccess; d++) {
-            e = launch_csr_spmv(dDs[d]->d, u, tt, stream);
-            if (e == cudaSuccess) e = launch_csr_spmv(dT[0]->d, tt, ss, stream);
-            if (e == cudaSuccess) e = launch_csr_spmv(dT[1]->d, ss, pp, stream);
-            if (e != cudaSuccess) break;
-            if (d < D)  // contrib1 = sum_d v_d .* x_d
-                e = launch_vlasov_combine(vp + (size_t)d * N, pp, d == 0 ? nullptr : a1, nullptr, a1, N, stream);
-            else if (d < P - 1)  // contrib2 = sum_d F_d .* p_d
-                e = launch_vlasov_combine(Fp + (size_t)(d - D) * N, pp, d == D ? nullptr : a2, nullptr, a2, N, stream);
-            else  // -contrib1 + contrib2
-                e = launch_vlasov_combine(Fp + (size_t)(d - D) * N, pp, d == D ? nullptr : a2, a1, a2, N, stream);
-        }
-        if (e == cudaSuccess) e = launch_csr_spmv(dT[2]->d, a2, zz, stream);
+        for (int d = 0; d < P && e == cudaSuccess; d++)
+            e = launch_csr_spmv_multi(dDs[d]->d, 1, u, 1, 0, tt + d, P, 0, stream);
+        if (e == cudaSuccess) e = launch_csr_spmv_multi(dT[0]->d, P, tt, P, 1, ss, P, 1, stream);
+        if (e == cudaSuccess) e = launch_csr_spmv_multi(dT[1]->d, P, ss, P, 1, pp, P, 1, stream);
+        if (e == cudaSuccess) e = launch_vlasov_points(vpt.as<double>(), F.as<double>(), pp, D, N, c.as<double>(), stream);
+        if (e == cudaSuccess) e = launch_csr_spmv(dT[2]->d, c.as<double>(), z.as<double>(), stream);
         return e;
     }
 };

@@ -1,6 +1,7 @@
-// device_csr.h -- an assembled operator on the device: CSR arrays plus the
-// long-row segments the SpMV kernels split rows of more than kCsrSplit
-// entries into (kernels.cu).
+// device_csr.h -- an assembled operator on the device: CSR arrays, the rows
+// binned by length (lanes per row of the CSR kernels) and the long-row
+// segments the kernels split rows of more than kCsrSplit entries into
+// (kernels.cu).
 #pragma once
 #include <algorithm>
 #include <memory>
@@ -13,21 +14,18 @@
 namespace sgdg {
 
 struct DeviceCSR {
-    DevBuf rowptr, col, val, long_row, long_seg, seg_begin, seg_end, partial;
+    DevBuf rowptr, col, val, bin_rows, long_row, long_seg, seg_begin, seg_end, partial;
     DevCSR d{};
 };
 
 constexpr int64_t kCsrSplit = 2048;  // entries a row group sums directly
 
-// lanes per row of the CSR kernels, from the mean row length
-inline int pick_vs(int64_t m, int64_t nnz) {
-    const double avg = m ? double(nnz) / double(m) : 0.0;
-    if (avg <= 2) return 1;
-    if (avg <= 4) return 2;
-    if (avg <= 10) return 4;
-    if (avg <= 24) return 8;
-    if (avg <= 48) return 16;
-    return 32;
+// bin of a row of L <= kCsrSplit entries: the fewest lanes 2^b (up to 32)
+// that give each lane at most four entries
+inline int csr_bin(int64_t L) {
+    int b = 0;
+    while (b + 1 < kCsrBins && (int64_t(4) << b) < L) b++;
+    return b;
 }
 
 // Fills D.d from D's buffers (already holding rowptr, col, val for m rows)
@@ -39,7 +37,36 @@ inline void finish_device_csr(DeviceCSR& D, const std::vector<int64_t>& rowptr, 
     D.d.rowptr = D.rowptr.as<int64_t>();
     D.d.col = D.col.as<int32_t>();
     D.d.val = D.val.as<double>();
-    D.d.vs = pick_vs(m, nnz);
+    // rows by bin (counting sort, ascending rows within a bin) and the
+    // blocks of 256 threads each bin takes
+    std::vector<int64_t> cnt(kCsrBins + 1, 0);
+    for (int64_t r = 0; r < m; r++) {
+        const int64_t L = rowptr[r + 1] - rowptr[r];
+        if (L <= kCsrSplit) cnt[csr_bin(L) + 1]++;
+    }
+    int64_t blocks = 0;
+    for (int b = 0; b < kCsrBins; b++) {
+        D.d.bin_block[b] = (int)blocks;
+        blocks += (cnt[b + 1] * (int64_t(1) << b) + 255) / 256;
+        cnt[b + 1] += cnt[b];
+        D.d.bin_first[b] = cnt[b];
+    }
+    if (blocks > (int64_t(1) << 30)) throw Error(SGDG_EINVAL, "operator too large for the CSR kernels");
+    D.d.bin_block[kCsrBins] = (int)blocks;
+    D.d.bin_first[kCsrBins] = cnt[kCsrBins];
+    std::vector<int32_t> rows((size_t)cnt[kCsrBins]);
+    {
+        std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+        for (int64_t r = 0; r < m; r++) {
+            const int64_t L = rowptr[r + 1] - rowptr[r];
+            if (L <= kCsrSplit) rows[(size_t)fill[csr_bin(L)]++] = (int32_t)r;
+        }
+    }
+    D.d.bin_rows = nullptr;
+    if (!rows.empty()) {
+        D.bin_rows = upload(rows, st);
+        D.d.bin_rows = D.bin_rows.as<int32_t>();
+    }
     std::vector<int32_t> lrow, lseg(1, 0);
     std::vector<int64_t> sb, se;
     for (int64_t r = 0; r < m; r++) {
@@ -60,7 +87,7 @@ inline void finish_device_csr(DeviceCSR& D, const std::vector<int64_t>& rowptr, 
         D.long_seg = upload(lseg, st);
         D.seg_begin = upload(sb, st);
         D.seg_end = upload(se, st);
-        D.partial.alloc(sizeof(double) * sb.size());
+        D.partial.alloc(sizeof(double) * sb.size() * kCsrMaxVec);
         D.d.long_row = D.long_row.as<int32_t>();
         D.d.long_seg = D.long_seg.as<int32_t>();
         D.d.seg_begin = D.seg_begin.as<int64_t>();

@@ -11,20 +11,28 @@ namespace sgdg {
 // warp each (partial sums in `partial`), then combined per row in segment
 // order -- so a handful of very long rows (a coarse mode touched by every
 // coefficient) does not serialise the launch, and results stay deterministic.
+constexpr int kCsrBins = 6;    // row bins of the CSR kernels: 1, 2, 4, ..., 32 lanes per row
+constexpr int kCsrMaxVec = 4;  // vectors one pass of the multi-vector SpMV carries
+
 struct DevCSR {
     int64_t m;
     int64_t nnz;
     const int64_t* rowptr;
     const int32_t* col;
     const double* val;
-    int vs;  // lanes per row
+    // rows of at most `split` entries by bin, ascending within a bin: bin b
+    // (2^b lanes per row) holds bin_rows[bin_first[b] .. bin_first[b + 1])
+    // and is served by grid blocks bin_block[b] .. bin_block[b + 1]
+    const int32_t* bin_rows;
+    int64_t bin_first[kCsrBins + 1];
+    int bin_block[kCsrBins + 1];
     int64_t split;            // longest row a single row group sums
     int64_t nlong, nseg;      // rows longer than split, their segments
     const int32_t* long_row;  // nlong: the rows
     const int32_t* long_seg;  // nlong + 1: first segment of each long row
-    const int64_t* seg_begin; // nseg + 1 style bounds: segment s is [seg_begin[s], seg_end[s])
+    const int64_t* seg_begin; // segment s is [seg_begin[s], seg_end[s])
     const int64_t* seg_end;
-    double* partial;          // nseg
+    double* partial;          // kCsrMaxVec * nseg: segment sums, one block of nseg per vector
 };
 
 // ---- chosen form: matrix-free FP32 pencil apply, FP64 RK state --------------

@@ -1,114 +1,212 @@
 // kernels.cu -- the plain form and small helpers.
 //
-//  * k_csr_spmv / k_csr_rk4: FP64 CSR mat-vec (the closure body *(RHS, x) of
-//    src/pdes.jl:63) with VS lanes per row; the RK4 variant fuses the
-//    classical stage combination into the row epilogue.  Rows longer than
-//    A.split are skipped there and summed by k_csr_segments (one warp per
-//    segment) and k_csr_long_rows (segment partials in order, then the same
-//    epilogue).
+//  * k_csr: FP64 CSR mat-vec (the closure body *(RHS, x) of src/pdes.jl:63)
+//    over NV vectors in one pass over A, or with NV = 1 fused with the
+//    classical RK4 stage combination.  Rows are binned by length
+//    (DevCSR.bin_*): a row of bin b gets 2^b lanes, each lane with four
+//    entries in flight, so the short and the long rows of one matrix (the
+//    nodal transforms hold both) keep the lanes equally busy; every block of
+//    the grid serves one bin.  Rows longer than A.split are summed by
+//    k_csr_segments (one warp per segment) and k_csr_long_rows (segment
+//    partials in order, then the same epilogue).
+//    Element (j, i) of the vector set x is x[i * xi + j * xs]: xi = 1 and
+//    xs = length for vectors one after another, xi = count and xs = 1 for
+//    interleaved vectors, whose values at one column share a sector and come
+//    in as one 32-byte (W = 4) or 16-byte (W = 2) load.
+//  * k_vlasov_points: the point-basis combination of the Vlasov right-hand side.
 //  * k_f64_to_f32 / k_f32_to_f64: precision conversions of whole vectors.
 #include <cuda_runtime.h>
+
+#include <cstdint>
 
 #include "engine.h"
 #include "rk.cuh"
 
 namespace sgdg {
 
-template <int VS>
-__device__ __forceinline__ double csr_row(const DevCSR& A, int64_t row, const double* __restrict__ x, int lane,
-                                          bool& long_row) {
-    double s = 0.0;
-    long_row = false;
-    if (row < A.m) {
+struct CsrRK {  // stage update of the RK4 epilogue: k = A uin, then rk_stage
+    double* acc;
+    double* uout;
+    double dt, hdt, dt6;
+    int stage;
+};
+
+// 256-bit read-only load (sm_100 and later); p 32-byte aligned
+__device__ __forceinline__ void ld_nc_v4(const double* p, double& a, double& b, double& c, double& d) {
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(a), "=d"(b), "=d"(c), "=d"(d) : "l"(p));
+}
+
+// the values of NV vectors at one column (element offset off = column * xi),
+// W adjacent vectors per load (W = 2: 16-byte, W = 4: 32-byte aligned)
+template <int NV, int W>
+__device__ __forceinline__ void csr_gather(const double* __restrict__ x, int64_t off, int64_t xs, double (&v)[NV]) {
+    if constexpr (W == 4) {
+#pragma unroll
+        for (int j = 0; j < NV; j += 4) ld_nc_v4(x + off + j, v[j], v[j + 1], v[j + 2], v[j + 3]);
+    } else if constexpr (W == 2) {
+#pragma unroll
+        for (int j = 0; j < NV; j += 2) {
+            const double2 t = __ldg(reinterpret_cast<const double2*>(x + off + j));
+            v[j] = t.x;
+            v[j + 1] = t.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < NV; j++) v[j] = __ldg(x + off + j * xs);
+    }
+}
+
+// s[j] = row `row` of A times vector j, summed over VS lanes (row < 0: zeros,
+// but the lanes still take part in the shuffles)
+template <int VS, int NV, int W>
+__device__ __forceinline__ void csr_row(const DevCSR& A, int64_t row, const double* __restrict__ x, int64_t xi,
+                                        int64_t xs, int lane, double (&s)[NV]) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) s[j] = 0.0;
+    if (row >= 0) {
         const int64_t b = A.rowptr[row], e = A.rowptr[row + 1];
-        long_row = e - b > A.split;
-        if (!long_row) {
-            // four entries per lane in flight: the column loads, then the gathers of x
-            int64_t p = b + lane;
-            for (; p + 3 * VS < e; p += 4 * VS) {
-                const int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + VS), c2 = __ldg(A.col + p + 2 * VS),
-                          c3 = __ldg(A.col + p + 3 * VS);
-                const double v0 = __ldg(A.val + p), v1 = __ldg(A.val + p + VS), v2 = __ldg(A.val + p + 2 * VS),
-                             v3 = __ldg(A.val + p + 3 * VS);
-                const double x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-                s = fma(v0, x0, s);
-                s = fma(v1, x1, s);
-                s = fma(v2, x2, s);
-                s = fma(v3, x3, s);
+        int64_t p = b + lane;
+        // four entries per lane in flight: the column loads, then the gathers of x
+        for (; p + 3 * VS < e; p += 4 * VS) {
+            const int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + VS), c2 = __ldg(A.col + p + 2 * VS),
+                      c3 = __ldg(A.col + p + 3 * VS);
+            const double v0 = __ldg(A.val + p), v1 = __ldg(A.val + p + VS), v2 = __ldg(A.val + p + 2 * VS),
+                         v3 = __ldg(A.val + p + 3 * VS);
+            double x0[NV], x1[NV], x2[NV], x3[NV];
+            csr_gather<NV, W>(x, c0 * xi, xs, x0);
+            csr_gather<NV, W>(x, c1 * xi, xs, x1);
+            csr_gather<NV, W>(x, c2 * xi, xs, x2);
+            csr_gather<NV, W>(x, c3 * xi, xs, x3);
+#pragma unroll
+            for (int j = 0; j < NV; j++) {
+                s[j] = fma(v0, x0[j], s[j]);
+                s[j] = fma(v1, x1[j], s[j]);
+                s[j] = fma(v2, x2[j], s[j]);
+                s[j] = fma(v3, x3[j], s[j]);
             }
-            for (; p < e; p += VS) s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
+        }
+        for (; p < e; p += VS) {
+            const int c = __ldg(A.col + p);
+            const double v = __ldg(A.val + p);
+            double xv[NV];
+            csr_gather<NV, W>(x, c * xi, xs, xv);
+#pragma unroll
+            for (int j = 0; j < NV; j++) s[j] = fma(v, xv[j], s[j]);
         }
     }
 #pragma unroll
-    for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    return s;
+    for (int j = 0; j < NV; j++)
+#pragma unroll
+        for (int o = VS / 2; o > 0; o >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
 }
 
-template <int VS>
-__global__ void __launch_bounds__(256) k_csr_spmv(DevCSR A, const double* __restrict__ x, double* __restrict__ y) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t row = t / VS;
-    const int lane = int(t % VS);
-    bool long_row;
-    double s = csr_row<VS>(A, row, x, lane, long_row);
-    if (row < A.m && lane == 0 && !long_row) y[row] = s;
+__device__ __forceinline__ void csr_rk_update(const CsrRK& rk, int64_t row, double k, double* y) {
+    double yy = y[row], aa = rk.stage == 1 ? 0.0 : rk.acc[row], un;
+    rk_stage(rk.stage, rk.dt, rk.hdt, rk.dt6, k, yy, aa, un);
+    if (rk.stage == 4)
+        y[row] = yy;
+    else {
+        rk.acc[row] = aa;
+        rk.uout[row] = un;
+    }
 }
 
-template <int VS>
-__global__ void __launch_bounds__(256) k_csr_rk4(DevCSR A, const double* uin, double* y, double* __restrict__ acc,
-                                                 double* __restrict__ uout, double dt, double hdt, double dt6,
-                                                 int stage) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t row = t / VS;
+// the rows of bin `bin`, 2^bin = VS lanes each
+template <int VS, int NV, int W, bool RK>
+__device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, const double* __restrict__ x, int64_t xi,
+                                        int64_t xs, double* y, int64_t yi, int64_t ys, const CsrRK& rk) {
+    const int64_t t = (int64_t)(blockIdx.x - A.bin_block[bin]) * blockDim.x + threadIdx.x;
+    const int64_t idx = t / VS, first = A.bin_first[bin];
     const int lane = int(t % VS);
-    bool long_row;
-    double k = csr_row<VS>(A, row, uin, lane, long_row);
-    if (row < A.m && lane == 0 && !long_row) {
-        double yy = y[row], aa = stage == 1 ? 0.0 : acc[row], un;
-        rk_stage(stage, dt, hdt, dt6, k, yy, aa, un);
-        if (stage == 4)
-            y[row] = yy;
+    const int64_t row = idx < A.bin_first[bin + 1] - first ? (int64_t)A.bin_rows[first + idx] : -1;
+    double s[NV];
+    csr_row<VS, NV, W>(A, row, x, xi, xs, lane, s);
+    if (row >= 0 && lane == 0) {
+        if constexpr (RK)
+            csr_rk_update(rk, row, s[0], y);
         else {
-            acc[row] = aa;
-            uout[row] = un;
+#pragma unroll
+            for (int j = 0; j < NV; j++) y[row * yi + j * ys] = s[j];
         }
     }
 }
 
-// one warp per segment of a long row
-__global__ void __launch_bounds__(256) k_csr_segments(DevCSR A, const double* __restrict__ x) {
+template <int NV, int W, bool RK>
+__global__ void __launch_bounds__(256) k_csr(DevCSR A, const double* __restrict__ x, int64_t xi, int64_t xs,
+                                             double* y, int64_t yi, int64_t ys, CsrRK rk) {
+    int bin = 0;
+    while (bin + 1 < kCsrBins && (int)blockIdx.x >= A.bin_block[bin + 1]) bin++;
+    switch (bin) {
+        case 0: csr_bin<1, NV, W, RK>(A, 0, x, xi, xs, y, yi, ys, rk); break;
+        case 1: csr_bin<2, NV, W, RK>(A, 1, x, xi, xs, y, yi, ys, rk); break;
+        case 2: csr_bin<4, NV, W, RK>(A, 2, x, xi, xs, y, yi, ys, rk); break;
+        case 3: csr_bin<8, NV, W, RK>(A, 3, x, xi, xs, y, yi, ys, rk); break;
+        case 4: csr_bin<16, NV, W, RK>(A, 4, x, xi, xs, y, yi, ys, rk); break;
+        default: csr_bin<32, NV, W, RK>(A, 5, x, xi, xs, y, yi, ys, rk); break;
+    }
+}
+
+// one warp per segment of a long row; partial sums of vector j at
+// A.partial[j * A.nseg + seg]
+template <int NV, int W>
+__global__ void __launch_bounds__(256) k_csr_segments(DevCSR A, const double* __restrict__ x, int64_t xi,
+                                                      int64_t xs) {
     const int64_t seg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (seg >= A.nseg) return;
-    double s = 0.0;
-    for (int64_t p = A.seg_begin[seg] + lane; p < A.seg_end[seg]; p += 32)
-        s = fma(__ldg(A.val + p), __ldg(x + __ldg(A.col + p)), s);
+    double s[NV];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) A.partial[seg] = s;
+    for (int j = 0; j < NV; j++) s[j] = 0.0;
+    const int64_t e = A.seg_end[seg];
+    int64_t p = A.seg_begin[seg] + lane;
+    for (; p + 96 < e; p += 128) {
+        const int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + 32), c2 = __ldg(A.col + p + 64),
+                  c3 = __ldg(A.col + p + 96);
+        const double v0 = __ldg(A.val + p), v1 = __ldg(A.val + p + 32), v2 = __ldg(A.val + p + 64),
+                     v3 = __ldg(A.val + p + 96);
+        double x0[NV], x1[NV], x2[NV], x3[NV];
+        csr_gather<NV, W>(x, c0 * xi, xs, x0);
+        csr_gather<NV, W>(x, c1 * xi, xs, x1);
+        csr_gather<NV, W>(x, c2 * xi, xs, x2);
+        csr_gather<NV, W>(x, c3 * xi, xs, x3);
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            s[j] = fma(v0, x0[j], s[j]);
+            s[j] = fma(v1, x1[j], s[j]);
+            s[j] = fma(v2, x2[j], s[j]);
+            s[j] = fma(v3, x3[j], s[j]);
+        }
+    }
+    for (; p < e; p += 32) {
+        const int c = __ldg(A.col + p);
+        const double v = __ldg(A.val + p);
+        double xv[NV];
+        csr_gather<NV, W>(x, c * xi, xs, xv);
+#pragma unroll
+        for (int j = 0; j < NV; j++) s[j] = fma(v, xv[j], s[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
+        if (lane == 0) A.partial[j * A.nseg + seg] = s[j];
+    }
 }
 
-// one thread per long row: its segments in order; y = A x, or the RK4 stage
-// update when acc is given
-__global__ void k_csr_long_rows(DevCSR A, double* y, double* acc, const double* uin, double* uout, double dt,
-                                double hdt, double dt6, int stage) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.nlong) return;
+// one thread per (long row, vector): the row's segment partials in order,
+// then the store or (rk_on, one vector) the RK4 stage update
+__global__ void k_csr_long_rows(DevCSR A, int nv, double* y, int64_t yi, int64_t ys, CsrRK rk, bool rk_on) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.nlong * nv) return;
+    const int64_t i = t % A.nlong;
+    const int j = int(t / A.nlong);
     double s = 0.0;
-    for (int q = A.long_seg[i]; q < A.long_seg[i + 1]; q++) s += A.partial[q];
+    for (int q = A.long_seg[i]; q < A.long_seg[i + 1]; q++) s += A.partial[j * A.nseg + q];
     const int64_t row = A.long_row[i];
-    if (!acc) {
-        y[row] = s;
-        return;
-    }
-    double yy = y[row], aa = stage == 1 ? 0.0 : acc[row], un;
-    rk_stage(stage, dt, hdt, dt6, s, yy, aa, un);
-    if (stage == 4)
-        y[row] = yy;
-    else {
-        acc[row] = aa;
-        uout[row] = un;
-    }
+    if (rk_on)
+        csr_rk_update(rk, row, s, y);
+    else
+        y[row * yi + j * ys] = s;
 }
 
 __global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
@@ -121,14 +219,21 @@ __global__ void k_f32_to_f64(const float* __restrict__ a, double* __restrict__ b
         b[i] = (double)a[i];
 }
 
-// Vlasov right-hand side in the point basis (src/pdes.jl:185-191):
-//   acc_out = (acc_in or 0) + w .* p; with `other` set, out = -other + acc_out.
-__global__ void k_vlasov_combine(const double* __restrict__ w, const double* __restrict__ p, const double* acc_in,
-                                 const double* __restrict__ other, double* out, int64_t n) {  // out may be acc_in
+// Vlasov right-hand side in the point basis (src/pdes.jl:185-191): with the
+// 2D transformed derivatives interleaved, pt[i * 2D + d] (x dimensions d < D,
+// then p),
+//   out = -(sum_d v_d .* pt_d) + sum_d F_d .* pt_{D+d},
+// each sum left to right with separate roundings of products and sums.
+__global__ void k_vlasov_points(const double* __restrict__ v, const double* __restrict__ F,
+                                const double* __restrict__ pt, int D, int64_t n, double* __restrict__ out) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double prod = w[i] * p[i];
-        const double a = acc_in ? acc_in[i] + prod : prod;
-        out[i] = other ? -other[i] + a : a;
+        const double* q = pt + i * 2 * D;
+        double c1 = __dmul_rn(v[i], q[0]), c2 = __dmul_rn(F[i], q[D]);
+        for (int d = 1; d < D; d++) {
+            c1 = __dadd_rn(c1, __dmul_rn(v[d * n + i], q[d]));
+            c2 = __dadd_rn(c2, __dmul_rn(F[d * n + i], q[D + d]));
+        }
+        out[i] = __dadd_rn(-c1, c2);
     }
 }
 
@@ -138,39 +243,55 @@ static int grid_for(int64_t threads) {
     return (int)(b > (1LL << 30) ? (1LL << 30) : (b < 1 ? 1 : b));
 }
 
-cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st) {
-    const int64_t th = A.m * A.vs;
-    switch (A.vs) {
-        case 1: k_csr_spmv<1><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
-        case 2: k_csr_spmv<2><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
-        case 4: k_csr_spmv<4><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
-        case 8: k_csr_spmv<8><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
-        case 16: k_csr_spmv<16><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
-        default: k_csr_spmv<32><<<grid_for(th), 256, 0, st>>>(A, x, y); break;
-    }
+template <int NV, int W, bool RK>
+static void csr_pass(const DevCSR& A, const double* x, int64_t xi, int64_t xs, double* y, int64_t yi, int64_t ys,
+                     const CsrRK& rk, cudaStream_t st) {
+    if (A.bin_block[kCsrBins] > 0) k_csr<NV, W, RK><<<A.bin_block[kCsrBins], 256, 0, st>>>(A, x, xi, xs, y, yi, ys, rk);
     if (A.nlong > 0) {
-        k_csr_segments<<<grid_for(A.nseg * 32), 256, 0, st>>>(A, x);
-        k_csr_long_rows<<<grid_for(A.nlong), 256, 0, st>>>(A, y, nullptr, nullptr, nullptr, 0.0, 0.0, 0.0, 0);
+        k_csr_segments<NV, W><<<grid_for(A.nseg * 32), 256, 0, st>>>(A, x, xi, xs);
+        k_csr_long_rows<<<grid_for(A.nlong * NV), 256, 0, st>>>(A, NV, y, yi, ys, rk, RK);
+    }
+}
+
+cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st) {
+    csr_pass<1, 1, false>(A, x, 1, 0, y, 1, 0, CsrRK{}, st);
+    return cudaGetLastError();
+}
+
+// y_j = A x_j for j < nv, kCsrMaxVec vectors per pass over A; element (j, i)
+// of x at x[i * xi + j * xs], of y at y[i * yi + j * ys]
+cudaError_t launch_csr_spmv_multi(const DevCSR& A, int nv, const double* x, int64_t xi, int64_t xs, double* y,
+                                  int64_t yi, int64_t ys, cudaStream_t st) {
+    for (int j = 0; j < nv; j += kCsrMaxVec) {
+        const double* xj = x + (int64_t)j * xs;
+        double* yj = y + (int64_t)j * ys;
+        const int w = nv - j < kCsrMaxVec ? nv - j : kCsrMaxVec;
+        // one load per column for adjacent vectors whose group is aligned at every column
+        const uintptr_t a = reinterpret_cast<uintptr_t>(xj);
+        const int wide = xs != 1 ? 1 : (w == 4 && xi % 4 == 0 && a % 32 == 0) ? 4 : (w % 2 == 0 && xi % 2 == 0 && a % 16 == 0) ? 2 : 1;
+        const CsrRK none{};
+        if (w == 4 && wide == 4)
+            csr_pass<4, 4, false>(A, xj, xi, xs, yj, yi, ys, none, st);
+        else if (w == 4 && wide == 2)
+            csr_pass<4, 2, false>(A, xj, xi, xs, yj, yi, ys, none, st);
+        else if (w == 4)
+            csr_pass<4, 1, false>(A, xj, xi, xs, yj, yi, ys, none, st);
+        else if (w == 3)
+            csr_pass<3, 1, false>(A, xj, xi, xs, yj, yi, ys, none, st);
+        else if (w == 2 && wide == 2)
+            csr_pass<2, 2, false>(A, xj, xi, xs, yj, yi, ys, none, st);
+        else if (w == 2)
+            csr_pass<2, 1, false>(A, xj, xi, xs, yj, yi, ys, none, st);
+        else
+            csr_pass<1, 1, false>(A, xj, xi, xs, yj, yi, ys, none, st);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
                            int stage, cudaStream_t st) {
-    const int64_t th = A.m * A.vs;
-    const double hdt = 0.5 * dt, dt6 = dt / 6.0;
-    switch (A.vs) {
-        case 1: k_csr_rk4<1><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
-        case 2: k_csr_rk4<2><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
-        case 4: k_csr_rk4<4><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
-        case 8: k_csr_rk4<8><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
-        case 16: k_csr_rk4<16><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
-        default: k_csr_rk4<32><<<grid_for(th), 256, 0, st>>>(A, uin, y, acc, uout, dt, hdt, dt6, stage); break;
-    }
-    if (A.nlong > 0) {
-        k_csr_segments<<<grid_for(A.nseg * 32), 256, 0, st>>>(A, uin);
-        k_csr_long_rows<<<grid_for(A.nlong), 256, 0, st>>>(A, y, acc, uin, uout, dt, hdt, dt6, stage);
-    }
+    const CsrRK rk{acc, uout, dt, 0.5 * dt, dt / 6.0, stage};
+    csr_pass<1, 1, true>(A, uin, 1, 0, y, 1, 0, rk, st);
     return cudaGetLastError();
 }
 
@@ -189,10 +310,10 @@ cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t
 }  // namespace sgdg
 
 namespace sgdg {
-cudaError_t launch_vlasov_combine(const double* w, const double* p, const double* acc_in, const double* other,
-                                  double* out, int64_t n, cudaStream_t st) {
+cudaError_t launch_vlasov_points(const double* v, const double* F, const double* pt, int D, int64_t n, double* out,
+                                 cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_vlasov_combine<<<grid_for(n) > 4096 ? 4096 : grid_for(n), 256, 0, st>>>(w, p, acc_in, other, out, n);
+    k_vlasov_points<<<grid_for(n) > 4096 ? 4096 : grid_for(n), 256, 0, st>>>(v, F, pt, D, n, out);
     return cudaGetLastError();
 }
 }  // namespace sgdg
