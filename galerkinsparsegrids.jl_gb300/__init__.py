@@ -13,6 +13,7 @@ are set-up and I/O around the hot path, like the reference's own set-up code.
 """
 import ctypes
 import functools
+import os
 
 import numpy as np
 import scipy.sparse as sp
@@ -564,13 +565,28 @@ class VlasovOperator:
         check(lib().sgdg_vlasov_rhs(self._h, self._force(F_point), np.ascontiguousarray(f, np.float64), out))
         return out
 
+    def write_h5(self, path="vlasov.h5", times=None, states=None):
+        """The file vlasov_evolve writes (src/pdes.jl:145-163, 217-223):
+        dimensions, order, levels; m2n, n2p, p2n, n2m and Ds[1] .. Ds[2D] as
+        SparseMatrixCSC fields (.m, .n, .colptr, .rowval 1-based, .nzval);
+        with a solution also times and f_modal.%06d.  HDF5, written on the
+        host."""
+        if times is None:
+            check(lib().sgdg_vlasov_write_h5(self._h, os.fsencode(path), 0, None, None))
+            return
+        t = np.ascontiguousarray(times, np.float64).reshape(-1)
+        S = np.ascontiguousarray(np.asarray(states, np.float64).reshape(t.size, self.N))
+        check(lib().sgdg_vlasov_write_h5(self._h, os.fsencode(path), t.size, t.ctypes.data, S.ctypes.data))
+
 
 def vlasov_evolve(D, k, n, F_point, f0_modal, time0, time1, nout=2, order="rk4", scheme="sparse", dt=None,
-                  nsteps=None, op=None, method="plain"):
+                  nsteps=None, op=None, method="plain", h5=None):
     """vlasov_evolve (src/pdes.jl:131-227) with classical RK4 and fixed steps:
     df/dt = -(v . grad_x f) + F . grad_p f, products taken in the point basis.
     ``F_point`` holds D arrays of point values.  method "plain": assembled
     FP64 sparse operators; "matfree": FP32 pencil sweeps, FP64 RK state.
+    ``h5``: a path (the reference always writes "vlasov.h5") to receive the
+    operators and the stored states as the reference writes them.
     Returns (times, states)."""
     _order(order)
     op = op or VlasovOperator(D, k, n, scheme)
@@ -582,6 +598,8 @@ def vlasov_evolve(D, k, n, F_point, f0_modal, time0, time1, nout=2, order="rk4",
     states = np.zeros((nout, op.N))
     check(lib().sgdg_vlasov_evolve(op._h, op._force(F_point), f0, float(time0), float(time1), ns, int(nout),
                                    _method(method), times, states.reshape(-1)))
+    if h5 is not None:
+        op.write_h5(h5, times, states)
     return times, list(states)
 
 

@@ -8,7 +8,7 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM_BUDGET, ETIMEOUT, ECUDA, ECANCELLED, ENOGPU, EUNSUPPORTED = range(8)
+OK, EINVAL, ENOMEM_BUDGET, ETIMEOUT, ECUDA, ECANCELLED, ENOGPU, EUNSUPPORTED, EIO = range(9)
 SCHEMES = {"sparse": 0, "full": 1}
 METHODS = {"plain": 0, "matfree": 1}
 KIND_ADVECT, KIND_WAVE = 0, 1
@@ -29,6 +29,7 @@ EXPORTS = [
     "sgdg_transform_device_export",
     "sgdg_vlasov_create", "sgdg_vlasov_destroy", "sgdg_vlasov_size", "sgdg_vlasov_v_point",
     "sgdg_vlasov_transform_nnz", "sgdg_vlasov_transform_export", "sgdg_vlasov_rhs", "sgdg_vlasov_evolve",
+    "sgdg_vlasov_write_h5",
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
     "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
     "sgdg_server_counts",
@@ -101,6 +102,7 @@ def lib(build=True):
     _sig(L, "sgdg_vlasov_transform_export", [_vp, _ci, _i64p, _i32p, _f64p])
     _sig(L, "sgdg_vlasov_rhs", [_vp, _f64p, _f64p, _f64p])
     _sig(L, "sgdg_vlasov_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
+    _sig(L, "sgdg_vlasov_write_h5", [_vp, ctypes.c_char_p, _c64, _vp, _vp])
     _sig(L, "sgdg_batch_add_vlasov", [_vp, _ci, _ci, _ci, _ci, _cd, _f64p, _f64p, ctypes.POINTER(_ci)])
     _sig(L, "sgdg_evaluate", [_ci, _ci, _ci, _ci, _f64p, _c64, _f64p, _f64p])
     _sig(L, "sgdg_evaluate_device", [_ci, _ci, _ci, _ci, _vp, _c64, _vp, _vp, _vp])

@@ -23,6 +23,7 @@ namespace sgdg {
 
 CSR assemble_dd(const SparseIndex& ix, const DLF1D& op, int d) {
     const int D = ix.D, k = ix.k;
+    if (d < 0 || d >= D) throw Error(1, "dimension out of range");
     CSR A;
     A.m = A.n = ix.N;
     A.rowptr.assign(ix.N + 1, 0);

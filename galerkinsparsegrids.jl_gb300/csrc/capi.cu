@@ -687,6 +687,37 @@ int sgdg_vlasov_transform_export(const sgdg_vlasov* v, int which, int64_t* rowpt
     API_END
 }
 
+int sgdg_vlasov_write_h5(const sgdg_vlasov* v, const char* path, int64_t nout, const double* times,
+                         const double* states) {
+    API_BEGIN
+    NEED(v);
+    NEED(path);
+    if (nout < 0) throw Error(SGDG_EINVAL, "nout must be >= 0");
+    if (nout > 0) {
+        NEED(times);
+        NEED(states);
+    }
+    H5Writer w(path);
+    w.scalar_i64("dimensions", v->D);
+    w.scalar_i64("order", v->k);
+    w.scalar_i64("levels", v->n);
+    static const char* names[4] = {"m2n", "n2p", "p2n", "n2m"};
+    for (int t = 0; t < 4; t++) h5_write_csc(w, names[t], v->host_transform(t));
+    for (int d = 0; d < v->P; d++)  // Ds[1] .. Ds[2D]: the 1-based names of the 0-based dimensions
+        h5_write_csc(w, "Ds[" + std::to_string(d + 1) + "]", assemble_dd(v->ix, *v->dlf, d));
+    if (nout > 0) {
+        const int64_t N = v->ix.N;
+        w.array_f64("times", times, nout);
+        for (int64_t i = 0; i < nout; i++) {
+            char name[32];
+            std::snprintf(name, sizeof name, "f_modal.%06lld", (long long)(i + 1));
+            w.array_f64(name, states + i * N, N);
+        }
+    }
+    w.close();
+    API_END
+}
+
 int sgdg_vlasov_rhs(sgdg_vlasov* v, const double* F_point, const double* f, double* out) {
     API_BEGIN
     NEED(v);

@@ -5,6 +5,7 @@
 // are 1-based in the public index map and 0-based inside the library.
 #pragma once
 #include <cstdint>
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -113,7 +114,7 @@ struct CSR {
     std::vector<double> val;
     int64_t nnz() const { return rowptr.empty() ? 0 : rowptr.back(); }
 };
-CSR assemble_dd(const SparseIndex& ix, const DLF1D& op, int d);              // D_matrix(D,d,k,n)
+CSR assemble_dd(const SparseIndex& ix, const DLF1D& op, int d);  // D_matrix(D, d + 1, k, n): d is 0-based
 CSR spgemm_sum(const std::vector<const CSR*>& A);                  // sum_i A_i * A_i
 CSR add_scaled(const std::vector<const CSR*>& A, const std::vector<double>& s);
 CSR wave_rhs(const CSR& lap);                                                // wave_data
@@ -131,6 +132,39 @@ CSR transform_1d(int k, int n, int which);                  // transform_1D
 CSR transform_dd(const SparseIndex& ix, const CSR& T1);      // transform(D, k, n, mat_1D)
 double nodal_point(int k, int L, int c, int m);                // collocation point of a point-basis index
 std::vector<double> vlasov_velocity_points(const SparseIndex& ix, int Dx);  // 2 p_d - 1, Dx x N
+
+// ------------------------------------------------------------ HDF5 out ----
+// Root-group datasets (64-bit integers, doubles; scalars and 1D arrays) in an
+// HDF5 file, as vlasov_evolve's vlasov.h5 holds them (h5write.cpp).
+class H5Writer {
+  public:
+    explicit H5Writer(const std::string& path);
+    ~H5Writer();
+    H5Writer(const H5Writer&) = delete;
+    H5Writer& operator=(const H5Writer&) = delete;
+    void scalar_i64(const std::string& name, int64_t v);
+    void array_i64(const std::string& name, const int64_t* v, int64_t n);
+    void array_f64(const std::string& name, const double* v, int64_t n);
+    void close();  // writes the metadata and the superblock
+
+  private:
+    static constexpr uint64_t kSuperblockBytes = 96;
+    struct Entry {
+        std::string name;
+        bool is_float;
+        int rank;
+        int64_t n;
+        uint64_t addr, bytes, oh;
+    };
+    void add(const std::string& name, bool is_float, int rank, int64_t n, const void* data);
+    void put(const void* p, uint64_t n);  // p == nullptr: zeros
+    void align8();
+    std::string path_;
+    std::FILE* f_ = nullptr;
+    uint64_t pos_ = 0;
+    std::vector<Entry> ents_;
+};
+void h5_write_csc(H5Writer& w, const std::string& name, const CSR& A);  // <name>.m, .n, .colptr, .rowval, .nzval
 
 // ------------------------------------------------------ pencil schedule ----
 // A pencil for dimension d fixes the levels of every other dimension; its

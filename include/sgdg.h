@@ -35,7 +35,8 @@ enum {
     SGDG_ECUDA = 4,           /* CUDA runtime error                                            */
     SGDG_ECANCELLED = 5,      /* the request was cancelled                                     */
     SGDG_ENOGPU = 6,          /* no usable CUDA device                                         */
-    SGDG_EUNSUPPORTED = 7     /* valid input outside what this build implements                */
+    SGDG_EUNSUPPORTED = 7,    /* valid input outside what this build implements                */
+    SGDG_EIO = 8              /* a file could not be opened or written                         */
 };
 
 enum { SGDG_SCHEME_SPARSE = 0, SGDG_SCHEME_FULL = 1 };
@@ -164,6 +165,16 @@ int sgdg_vlasov_rhs(sgdg_vlasov *v, const double *F_point, const double *f, doub
  * RK state. */
 int sgdg_vlasov_evolve(sgdg_vlasov *v, const double *F_point, const double *f0, double t0, double t1, int64_t nsteps,
                        int nout, int method, double *times, double *states);
+/* The file vlasov_evolve writes, vlasov.h5 (src/pdes.jl:145-163 and
+ * 217-223), at `path`: the Int64 scalars "dimensions", "order", "levels";
+ * for m2n, n2p, p2n, n2m and Ds[1] .. Ds[2D] (grad_matrix(2D, k, n)) the
+ * SparseMatrixCSC fields "<name>.m", ".n", ".colptr", ".rowval" (Int64,
+ * 1-based) and ".nzval" (Float64); then "times" (nout) and "f_modal.%06d"
+ * (i = 1..nout, N each, the rows of `states`).  nout = 0 writes the operators
+ * only.  HDF5 with an old-style root group; SGDG_EIO when the file cannot be
+ * written.  Host only. */
+int sgdg_vlasov_write_h5(const sgdg_vlasov *v, const char *path, int64_t nout, const double *times,
+                         const double *states);
 
 /* ---- batches of independent solves (matrix-free form) ------------------- */
 /* Many solves of uneven D, k, n advance together: each RK stage is one
