@@ -21,10 +21,11 @@ struct DeviceCSR {
 constexpr int64_t kCsrSplit = 2048;  // entries a row group sums directly
 
 // bin of a row of L <= kCsrSplit entries: the fewest lanes 2^b (up to 32)
-// that give each lane at most four entries
+// that give each lane at most eight entries (fewer lanes per row: fewer FP64
+// additions in the lane reduction, which on GB300 cost as much as the FMAs)
 inline int csr_bin(int64_t L) {
     int b = 0;
-    while (b + 1 < kCsrBins && (int64_t(4) << b) < L) b++;
+    while (b + 1 < kCsrBins && (int64_t(8) << b) < L) b++;
     return b;
 }
 

@@ -3,10 +3,12 @@
 //  * k_csr: FP64 CSR mat-vec (the closure body *(RHS, x) of src/pdes.jl:63)
 //    over NV vectors in one pass over A, or with NV = 1 fused with the
 //    classical RK4 stage combination.  Rows are binned by length
-//    (DevCSR.bin_*): a row of bin b gets 2^b lanes, each lane with four
-//    entries in flight, so the short and the long rows of one matrix (the
-//    nodal transforms hold both) keep the lanes equally busy; every block of
-//    the grid serves one bin.  Rows longer than A.split are summed by
+//    (DevCSR.bin_*): a row of bin b gets 2^b lanes with at most eight entries
+//    each (four in flight), so the short and the long rows of one matrix (the
+//    nodal transforms hold both) keep the lanes equally busy and the lane
+//    reduction (csr_reduce) stays small against the FMAs -- on GB300 both run
+//    on the FP64 pipe, which bounds these kernels; every block of the grid
+//    serves one bin.  Rows longer than A.split are summed by
 //    k_csr_segments (one warp per segment) and k_csr_long_rows (segment
 //    partials in order, then the same epilogue).
 //    Element (j, i) of the vector set x is x[i * xi + j * xs]: xi = 1 and
@@ -56,8 +58,70 @@ __device__ __forceinline__ void csr_gather(const double* __restrict__ x, int64_t
     }
 }
 
+// Sum of s[0..NV) over the VS lanes of a row group.  With NV = 2 or 4 the
+// first steps exchange halves of the vector set instead of every value (a
+// lane keeps the half selected by its lane bit and adds its partner's copy),
+// so a row costs log2(VS) + NV - 2 FP64 additions per lane instead of
+// NV log2(VS); each vector's sum has the pairing, and therefore the value, of
+// the all-lane butterfly.  On return vector j's sum is in s[0] of the lanes
+// whose group index has j in its top bits (csr_owner), or in s[j] of every
+// lane when there was nothing to exchange (NV = 1 or 3, or VS too small).
+template <int VS, int NV>
+__device__ __forceinline__ void csr_reduce(double (&s)[NV], int lane) {
+    if constexpr ((NV == 4 && VS >= 4) || (NV == 2 && VS >= 2)) {
+        constexpr int o1 = VS / 2;
+        const bool up1 = lane & o1;
+        double h[NV / 2];
+#pragma unroll
+        for (int i = 0; i < NV / 2; i++) {
+            const double keep = up1 ? s[NV / 2 + i] : s[i];
+            const double give = up1 ? s[i] : s[NV / 2 + i];
+            h[i] = keep + __shfl_xor_sync(0xffffffffu, give, o1);
+        }
+        double r;
+        int o;
+        if constexpr (NV == 4) {
+            constexpr int o2 = VS / 4;
+            const bool up2 = lane & o2;
+            const double keep = up2 ? h[1] : h[0];
+            const double give = up2 ? h[0] : h[1];
+            r = keep + __shfl_xor_sync(0xffffffffu, give, o2);
+            o = VS / 8;
+        } else {
+            r = h[0];
+            o = VS / 4;
+        }
+        for (; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+        s[0] = r;
+    } else {
+#pragma unroll
+        for (int j = 0; j < NV; j++)
+#pragma unroll
+            for (int o = VS / 2; o > 0; o >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
+    }
+}
+
+// Which vector's sum the lane holds after csr_reduce (-1: all of them, in
+// s[j]); only lanes whose low bits are zero store it.
+template <int VS, int NV>
+__device__ __forceinline__ int csr_owner(int lane, bool& stores) {
+    if constexpr ((NV == 4 && VS >= 4) || (NV == 2 && VS >= 2)) {
+        constexpr int per = VS / NV;  // lanes holding one vector's sum
+        stores = lane % per == 0;
+        // vector index: bit VS/2 selects the upper half of the set, then bit VS/4 within it
+        if constexpr (NV == 4)
+            return ((lane & (VS / 2)) ? 2 : 0) + ((lane & (VS / 4)) ? 1 : 0);
+        else
+            return (lane & (VS / 2)) ? 1 : 0;
+    } else {
+        stores = lane == 0;
+        return -1;
+    }
+}
+
 // s[j] = row `row` of A times vector j, summed over VS lanes (row < 0: zeros,
-// but the lanes still take part in the shuffles)
+// but the lanes still take part in the shuffles); see csr_reduce for where
+// the sums end up
 template <int VS, int NV, int W>
 __device__ __forceinline__ void csr_row(const DevCSR& A, int64_t row, const double* __restrict__ x, int64_t xi,
                                         int64_t xs, int lane, double (&s)[NV]) {
@@ -94,10 +158,7 @@ __device__ __forceinline__ void csr_row(const DevCSR& A, int64_t row, const doub
             for (int j = 0; j < NV; j++) s[j] = fma(v, xv[j], s[j]);
         }
     }
-#pragma unroll
-    for (int j = 0; j < NV; j++)
-#pragma unroll
-        for (int o = VS / 2; o > 0; o >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
+    csr_reduce<VS, NV>(s, lane);
 }
 
 __device__ __forceinline__ void csr_rk_update(const CsrRK& rk, int64_t row, double k, double* y) {
@@ -121,9 +182,13 @@ __device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, const double* 
     const int64_t row = idx < A.bin_first[bin + 1] - first ? (int64_t)A.bin_rows[first + idx] : -1;
     double s[NV];
     csr_row<VS, NV, W>(A, row, x, xi, xs, lane, s);
-    if (row >= 0 && lane == 0) {
+    bool stores;
+    const int owner = csr_owner<VS, NV>(lane, stores);
+    if (row >= 0 && stores) {
         if constexpr (RK)
             csr_rk_update(rk, row, s[0], y);
+        else if (owner >= 0)
+            y[row * yi + owner * ys] = s[0];
         else {
 #pragma unroll
             for (int j = 0; j < NV; j++) y[row * yi + j * ys] = s[j];
@@ -185,11 +250,16 @@ __global__ void __launch_bounds__(256) k_csr_segments(DevCSR A, const double* __
 #pragma unroll
         for (int j = 0; j < NV; j++) s[j] = fma(v, xv[j], s[j]);
     }
+    csr_reduce<32, NV>(s, lane);
+    bool stores;
+    const int owner = csr_owner<32, NV>(lane, stores);
+    if (stores) {
+        if (owner >= 0)
+            A.partial[owner * A.nseg + seg] = s[0];
+        else {
 #pragma unroll
-    for (int j = 0; j < NV; j++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
-        if (lane == 0) A.partial[j * A.nseg + seg] = s[j];
+            for (int j = 0; j < NV; j++) A.partial[j * A.nseg + seg] = s[j];
+        }
     }
 }
 
