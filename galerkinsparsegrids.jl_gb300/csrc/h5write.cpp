@@ -160,7 +160,8 @@ void H5Writer::close() {
         }
         message(msgs, 0x0003, 1, m);
         m.b.clear();
-        // fill value, version 2: allocated early, never written, undefined
+        // fill value, version 2: space allocated early, fill written only if
+        // one is set (write time 2), none set
         m.u8(2);
         m.u8(1);
         m.u8(2);
