@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--solves", type=int, default=256)
     p.add_argument("--e2e-steps", type=int, default=5)
-    p.add_argument("--e2e-chunks", type=int, default=8, help="pipeline chunks of the end-to-end leg")
+    p.add_argument("--e2e-chunks", type=int, default=16, help="pipeline chunks of the end-to-end leg")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--vlasov-steps", type=int, default=500, help="RK4 steps of the 2x2v Vlasov leg (0: skip)")
     p.add_argument("--serve-requests", type=int, default=32, help="requests in the serving stream (0: skip)")

@@ -755,7 +755,7 @@ class Batch:
         """All live states into host memory at address ``ptr`` (synchronises)."""
         check(lib().sgdg_batch_download(self._h, ctypes.c_void_p(ptr)))
 
-    def step_host(self, y_in, y_out=None, nsteps=1, chunks=8):
+    def step_host(self, y_in, y_out=None, nsteps=1, chunks=16):
         """Every live state from host memory, ``nsteps`` RK4 steps, the results
         back (id order, like upload/download).  ``y_in`` / ``y_out`` are
         addresses of float64 host memory (pinned for the copies to overlap the

@@ -711,6 +711,10 @@ void MFEngine::build_chunks(int nchunks) {
     chunks_.resize(nchunks);
     const size_t smem = smem_;
     const int tb = table_bytes_;
+    // a chunk holds a fraction of the groups, so its phases wait on one
+    // another more; with half the persistent grid per launch two chunks' stage
+    // launches run side by side and cover each other's waits
+    const int cgrid = nchunks > 1 ? std::max(1, grid_ / 2) : grid_;
     for (int ci = 0; ci < nchunks; ci++) {
         Chunk& ch = chunks_[ci];
         std::vector<MFItem> items;
@@ -729,7 +733,7 @@ void MFEngine::build_chunks(int nchunks) {
         cudaError_t err = cudaSuccess;
         for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
             err = launch_mf_stage(ch.items.as<MFItem>(), ch.nitems, classes_d_.as<MFClass>(), ch.ctr.as<int>(), ch.nctr,
-                                  stage, (stage - 1) % 2, err_d_.as<int>(), smem_, table_bytes_, grid_, ch.st);
+                                  stage, (stage - 1) % 2, err_d_.as<int>(), smem_, table_bytes_, cgrid, ch.st);
         cudaError_t e2 = cudaStreamEndCapture(ch.st, &g);
         if (err != cudaSuccess || e2 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
