@@ -255,7 +255,8 @@ std::unique_ptr<DeviceCSR> merge_terms(const std::vector<const DeviceCSR*>& term
 // each with dimension 0 varying fastest, which is the order of the global
 // index (level blocks in CartesianIndices order, then cells, then modes), so
 // the row comes out sorted.
-constexpr int kTLev = 16;  // levels per dimension (n + 1)
+constexpr int kTLev = 16;         // levels per dimension (n + 1)
+constexpr int kTRowsPerBlock = 8;  // k_transform: one warp per row
 
 struct TransArgs {
     int D, k, n, scheme, nlev;
@@ -275,156 +276,186 @@ __device__ __forceinline__ void dec1d(int k, int j1, int& L, int& c, int& m) {
     c = L >= 2 ? blk - (1 << (L - 2)) : 0;     // 0-based cell
 }
 
+// the cell-tuple group of dimension d that starts at entry cs: its end
+__device__ __forceinline__ int cell_group_end(const TransArgs& A, int cs, int gend) {
+    int L0, c0, m0;
+    dec1d(A.k, A.col1[cs], L0, c0, m0);
+    int ce = cs;
+    while (ce < gend) {
+        int L, c, m;
+        dec1d(A.k, A.col1[ce], L, c, m);
+        if (c != c0) break;
+        ce++;
+    }
+    return ce;
+}
+
+// Entries of row i in level tuple g (group g[d] of every dimension's 1D row):
+// nothing when the tuple is cut or not on the grid, else the cell tuples and
+// within them the mode tuples (dimension 0 fastest), products |v| >= 1e-12.
+// Returns the count; with FILL also writes them from position w on (never at
+// or past lim).
 template <bool FILL>
-__global__ void k_transform(TransArgs A, int32_t* rowlen, const int64_t* __restrict__ rowptr,
-                            int32_t* __restrict__ col, double* __restrict__ val) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.N) return;
+__device__ int32_t tuple_entries(const TransArgs& A, const int* g, const int (*gs)[kTLev], const int (*ge)[kTLev],
+                                 const int (*gl)[kTLev], int64_t w, int64_t lim, int32_t* __restrict__ col,
+                                 double* __restrict__ val) {
     const int D = A.D, k = A.k;
-    // (level, cell, mode) of row i per dimension -> its 1D row
-    int lo = 0, hi = A.nlev - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (A.lev_off[mid] <= i) lo = mid; else hi = mid - 1;
-    }
-    const int8_t* Li = A.levels + (size_t)lo * D;
-    int64_t cl = (i - A.lev_off[lo]) / A.kD, ml = (i - A.lev_off[lo]) % A.kD;
-    int a[8], b[8];  // each dimension's 1D row (entry indices; 1D transforms hold < 2^31 entries)
+    int code = 0, lsum = 0, mult = 1;
     for (int d = 0; d < D; d++) {
-        const int L = Li[d];
-        const int64_t nc = (int64_t)1 << (L > 2 ? L - 2 : 0);
-        const int64_t c = cl % nc, m = ml % k;
-        cl /= nc;
-        ml /= k;
-        const int64_t i1 = k * ((L >= 2 ? ((int64_t)1 << (L - 2)) : 0) + c) + m;
-        a[d] = (int)A.rp1[i1];
-        b[d] = (int)A.rp1[i1 + 1];
+        code += (gl[d][g[d]] - 1) * mult;
+        mult *= A.n + 1;
+        lsum += gl[d][g[d]];
     }
-    // level groups of each 1D row: [gs, ge) entries of level gl
-    int ng[8];
-    int gs[8][kTLev], ge[8][kTLev], gl[8][kTLev];
-    for (int d = 0; d < D; d++) {
-        ng[d] = 0;
-        int last = -1;
-        for (int e = a[d]; e < b[d]; e++) {
-            int L, c, m;
-            dec1d(k, A.col1[e], L, c, m);
-            if (L != last) {
-                gs[d][ng[d]] = e;
-                gl[d][ng[d]] = L;
-                if (ng[d] > 0) ge[d][ng[d] - 1] = e;
-                ng[d]++;
-                last = L;
-            }
-        }
-        if (ng[d] == 0) {  // an empty 1D row: no entries in row i
-            if (!FILL) rowlen[i] = 0;
-            return;
-        }
-        ge[d][ng[d] - 1] = b[d];
-    }
-    int64_t w = FILL ? rowptr[i] : 0;
+    const int blk = (A.scheme == 0 && lsum > A.n + D) ? -1 : A.code2lev[code];
+    if (blk < 0) return 0;
+    const int64_t base = A.lev_off[blk];
     int32_t cnt = 0;
-    int g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (;;) {  // level tuples, dimension 0 fastest
-        int code = 0, lsum = 0, mult = 1;
+    int cs[8], ce[8];
+    for (int d = 0; d < D; d++) {
+        cs[d] = gs[d][g[d]];
+        ce[d] = cell_group_end(A, cs[d], ge[d][g[d]]);
+    }
+    for (;;) {  // cell tuples
+        int64_t cell_lin = 0, cstride = 1;
         for (int d = 0; d < D; d++) {
-            code += (gl[d][g[d]] - 1) * mult;
-            mult *= A.n + 1;
-            lsum += gl[d][g[d]];
+            int L, c, m;
+            dec1d(k, A.col1[cs[d]], L, c, m);
+            cell_lin += (int64_t)c * cstride;
+            cstride <<= (L > 2 ? L - 2 : 0);
         }
-        const int blk = (A.scheme == 0 && lsum > A.n + D) ? -1 : A.code2lev[code];
-        if (blk >= 0) {
-            const int64_t base = A.lev_off[blk];
-            // cell tuples within the groups: cs = first entry of the cell group, ce its end
-            int cs[8], ce[8];
+        int e[8];
+        for (int d = 0; d < D; d++) e[d] = cs[d];
+        for (;;) {  // mode tuples
+            double v = 1.0;
             for (int d = 0; d < D; d++) {
-                cs[d] = gs[d][g[d]];
-                ce[d] = cs[d];
-                int L0, c0, m0;
-                dec1d(k, A.col1[cs[d]], L0, c0, m0);
-                while (ce[d] < ge[d][g[d]]) {
-                    int L, c, m;
-                    dec1d(k, A.col1[ce[d]], L, c, m);
-                    if (c != c0) break;
-                    ce[d]++;
-                }
+                v = __dmul_rn(v, A.val1[e[d]]);
+                if (v == 0.0) break;
             }
-            for (;;) {
-                int64_t cell_lin = 0, cstride = 1;
-                for (int d = 0; d < D; d++) {
-                    int L, c, m;
-                    dec1d(k, A.col1[cs[d]], L, c, m);
-                    cell_lin += (int64_t)c * cstride;
-                    cstride <<= (L > 2 ? L - 2 : 0);
-                }
-                // mode tuples within the cell groups
-                int e[8];
-                for (int d = 0; d < D; d++) e[d] = cs[d];
-                for (;;) {
-                    double v = 1.0;
+            if (!(fabs(v) < 1e-12)) {
+                if (FILL && w + cnt < lim) {
+                    int64_t mode_lin = 0, ms = 1;
                     for (int d = 0; d < D; d++) {
-                        v = __dmul_rn(v, A.val1[e[d]]);
-                        if (v == 0.0) break;
-                    }
-                    if (!(fabs(v) < 1e-12)) {
-                        if (FILL) {
-                            int64_t mode_lin = 0, ms = 1;
-                            for (int d = 0; d < D; d++) {
-                                int L, c, m;
-                                dec1d(k, A.col1[e[d]], L, c, m);
-                                mode_lin += m * ms;
-                                ms *= k;
-                            }
-                            col[w] = (int32_t)(base + A.kD * cell_lin + mode_lin);
-                            val[w] = v;
-                            w++;
-                        }
-                        cnt++;
-                    }
-                    int d = 0;
-                    for (; d < D; d++) {  // next mode tuple
-                        if (++e[d] < ce[d]) break;
-                        e[d] = cs[d];
-                    }
-                    if (d == D) break;
-                }
-                int d = 0;
-                for (; d < D; d++) {  // next cell tuple
-                    if (ce[d] < ge[d][g[d]]) {
-                        cs[d] = ce[d];
-                        int L0, c0, m0;
-                        dec1d(k, A.col1[cs[d]], L0, c0, m0);
-                        while (ce[d] < ge[d][g[d]]) {
-                            int L, c, m;
-                            dec1d(k, A.col1[ce[d]], L, c, m);
-                            if (c != c0) break;
-                            ce[d]++;
-                        }
-                        break;
-                    }
-                    cs[d] = gs[d][g[d]];  // wrap to the first cell group of the level
-                    ce[d] = cs[d];
-                    int L0, c0, m0;
-                    dec1d(k, A.col1[cs[d]], L0, c0, m0);
-                    while (ce[d] < ge[d][g[d]]) {
                         int L, c, m;
-                        dec1d(k, A.col1[ce[d]], L, c, m);
-                        if (c != c0) break;
-                        ce[d]++;
+                        dec1d(k, A.col1[e[d]], L, c, m);
+                        mode_lin += m * ms;
+                        ms *= k;
                     }
+                    col[w + cnt] = (int32_t)(base + A.kD * cell_lin + mode_lin);
+                    val[w + cnt] = v;
                 }
-                if (d == D) break;
+                cnt++;
             }
+            int d = 0;
+            for (; d < D; d++) {
+                if (++e[d] < ce[d]) break;
+                e[d] = cs[d];
+            }
+            if (d == D) break;
         }
         int d = 0;
-        for (; d < D; d++) {  // next level tuple
-            if (++g[d] < ng[d]) break;
-            g[d] = 0;
+        for (; d < D; d++) {  // next cell tuple
+            if (ce[d] < ge[d][g[d]]) {
+                cs[d] = ce[d];
+                ce[d] = cell_group_end(A, cs[d], ge[d][g[d]]);
+                break;
+            }
+            cs[d] = gs[d][g[d]];  // wrap to the first cell group of the level
+            ce[d] = cell_group_end(A, cs[d], ge[d][g[d]]);
         }
         if (d == D) break;
     }
-    if (!FILL) rowlen[i] = cnt;
+    return cnt;
+}
+
+// One warp per row.  The row's level tuples (dimension 0 fastest, the order
+// of the global index) are taken 32 at a time, one per lane; a warp scan of
+// the lanes' entry counts places each lane's entries, so rounds and lanes
+// write the row in order.  Rows differ by four orders of magnitude in length
+// (a coarse modal row of n2m spans the whole grid), and the lanes split a long
+// row's tuples instead of one thread walking it.  The level groups of the
+// row's 1D rows (one lane per dimension builds them) live in shared memory,
+// one copy per warp.
+template <bool FILL>
+__global__ void __launch_bounds__(32 * kTRowsPerBlock)
+    k_transform(TransArgs A, int32_t* rowlen, const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
+                double* __restrict__ val) {
+    __shared__ int s_grp[kTRowsPerBlock][3][8][kTLev];  // per warp: gs, ge, gl
+    __shared__ int s_ng[kTRowsPerBlock][8];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * kTRowsPerBlock + wib;
+    if (i >= A.N) return;  // the whole warp
+    const int D = A.D, k = A.k;
+    int(*gs)[kTLev] = s_grp[wib][0];
+    int(*ge)[kTLev] = s_grp[wib][1];
+    int(*gl)[kTLev] = s_grp[wib][2];
+    int* ng = s_ng[wib];
+    if (lane < D) {
+        // (level, cell, mode) of row i along dimension `lane` -> its 1D row
+        int lo = 0, hi = A.nlev - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (A.lev_off[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        const int8_t* Li = A.levels + (size_t)lo * D;
+        int64_t cl = (i - A.lev_off[lo]) / A.kD, ml = (i - A.lev_off[lo]) % A.kD;
+        int64_t i1 = 0;
+        for (int d = 0; d <= lane; d++) {
+            const int L = Li[d];
+            const int64_t nc = (int64_t)1 << (L > 2 ? L - 2 : 0);
+            const int64_t c = cl % nc, m = ml % k;
+            cl /= nc;
+            ml /= k;
+            i1 = k * ((L >= 2 ? ((int64_t)1 << (L - 2)) : 0) + c) + m;
+        }
+        const int a = (int)A.rp1[i1], b = (int)A.rp1[i1 + 1];  // 1D transforms hold < 2^31 entries
+        // level groups of the 1D row: [gs, ge) entries of level gl
+        int n = 0, last = -1;
+        for (int e = a; e < b; e++) {
+            int L, c, m;
+            dec1d(k, A.col1[e], L, c, m);
+            if (L != last) {
+                gs[lane][n] = e;
+                gl[lane][n] = L;
+                if (n > 0) ge[lane][n - 1] = e;
+                n++;
+                last = L;
+            }
+        }
+        if (n > 0) ge[lane][n - 1] = b;
+        ng[lane] = n;
+    }
+    __syncwarp();
+    int64_t ntup = 1;
+    for (int d = 0; d < D; d++) ntup *= ng[d];
+    if (ntup == 0) {  // an empty 1D row: no entries in row i
+        if (!FILL && lane == 0) rowlen[i] = 0;
+        return;  // the whole warp
+    }
+    int64_t w = FILL ? rowptr[i] : 0;
+    const int64_t lim = FILL ? rowptr[i + 1] : 0;
+    for (int64_t t0 = 0; t0 < ntup; t0 += 32) {
+        const int64_t t = t0 + lane;
+        int g[8];
+        int32_t c = 0;
+        if (t < ntup) {
+            int64_t r = t;
+            for (int d = 0; d < D; d++) {
+                g[d] = (int)(r % ng[d]);
+                r /= ng[d];
+            }
+            c = tuple_entries<false>(A, g, gs, ge, gl, 0, 0, nullptr, nullptr);
+        }
+        int32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int32_t rsum = __shfl_sync(0xffffffffu, incl, 31);
+        if (FILL && c > 0) tuple_entries<true>(A, g, gs, ge, gl, w + incl - c, lim, col, val);
+        w += rsum;
+    }
+    if (!FILL && lane == 0) rowlen[i] = (int32_t)w;
 }
 
 }  // namespace
@@ -476,15 +507,16 @@ std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, c
     TransArgs A{D, k, n, ix.scheme, ix.nlev, ix.N, ix.kD, d_lv.as<int8_t>(), d_lo.as<int32_t>(), d_code.as<int32_t>(),
                 d_rp.as<int64_t>(), d_cl.as<int32_t>(), d_vl.as<double>()};
     DevBuf rowlen(sizeof(int32_t) * (size_t)ix.N);
-    k_transform<false><<<grid_for(ix.N), 256, 0, st>>>(A, rowlen.as<int32_t>(), nullptr, nullptr, nullptr);
+    const int tgrid = (int)((ix.N + kTRowsPerBlock - 1) / kTRowsPerBlock);
+    k_transform<false><<<tgrid, 32 * kTRowsPerBlock, 0, st>>>(A, rowlen.as<int32_t>(), nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
     std::vector<int64_t> rph = scan_rows(rowlen, ix.N, st);
     auto R = std::make_unique<DeviceCSR>();
     R->rowptr = upload(rph, st);
     R->col.alloc(sizeof(int32_t) * (size_t)rph[ix.N]);
     R->val.alloc(sizeof(double) * (size_t)rph[ix.N]);
-    k_transform<true><<<grid_for(ix.N), 256, 0, st>>>(A, nullptr, R->rowptr.as<int64_t>(), R->col.as<int32_t>(),
-                                                      R->val.as<double>());
+    k_transform<true><<<tgrid, 32 * kTRowsPerBlock, 0, st>>>(A, nullptr, R->rowptr.as<int64_t>(),
+                                                              R->col.as<int32_t>(), R->val.as<double>());
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     finish_device_csr(*R, rph, ix.N, st);
