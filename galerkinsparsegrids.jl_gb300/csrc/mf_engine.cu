@@ -367,6 +367,7 @@ void MFEngine::plan() {
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     grid_ = std::max(1, bps) * sms;
+    sms_ = sms;
     CK(cudaStreamSynchronize(stream_));
     dirty_ = false;
 }
@@ -712,9 +713,10 @@ void MFEngine::build_chunks(int nchunks) {
     const size_t smem = smem_;
     const int tb = table_bytes_;
     // a chunk holds a fraction of the groups, so its phases wait on one
-    // another more; with half the persistent grid per launch two chunks' stage
-    // launches run side by side and cover each other's waits
-    const int cgrid = nchunks > 1 ? std::max(1, grid_ / 2) : grid_;
+    // another more; with one CTA per SM per launch, as many chunks' stage
+    // launches as CTAs fit on an SM run side by side and cover each other's
+    // waits
+    const int cgrid = nchunks > 1 ? std::max(1, sms_) : grid_;
     for (int ci = 0; ci < nchunks; ci++) {
         Chunk& ch = chunks_[ci];
         std::vector<MFItem> items;

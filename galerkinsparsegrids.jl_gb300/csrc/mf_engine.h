@@ -117,7 +117,7 @@ class MFEngine {
     std::map<std::pair<int, int>, STable> stabs_;
     std::map<std::pair<int, int>, TTables> ttabs_;
     DevBuf classes_d_, items_d_, ctr_d_, err_d_;
-    int nitems_ = 0, nctr_ = 0, grid_ = 0;
+    int nitems_ = 0, nctr_ = 0, grid_ = 0, sms_ = 0;  // grid_: resident CTAs per SM x SMs
     int64_t pending_bytes_ = 0;  // admitted but not yet allocated
     size_t smem_ = 0;
     int table_bytes_ = 0;  // shared-memory operator table reserved ahead of the tile
