@@ -212,9 +212,11 @@ int sgdg_batch_upload(sgdg_batch *b, const double *y_all);
 int sgdg_batch_download(sgdg_batch *b, double *y_all);
 /* Host states in, RK4 steps, host states out (same layout as upload/download;
  * y_out may equal y_in), in one call that synchronises.  The batch's groups
- * of solves are split into nchunks pipeline chunks on their own streams, so
- * one chunk's host<->device copies overlap the other chunks' steps; pinned
- * host memory is needed for the copies to overlap. */
+ * of solves are split into nchunks (1..64) pipeline chunks on their own
+ * streams, so one chunk's host<->device copies overlap the other chunks'
+ * steps; a chunk's stage launches take one CTA per SM, so several chunks step
+ * side by side.  16 chunks suit a batch of a few hundred solves.  Pinned host
+ * memory is needed for the copies to overlap. */
 int sgdg_batch_step_host(sgdg_batch *b, const double *y_in, double *y_out, int64_t nsteps, int nchunks);
 /* Autotuner: for every (D, k) of the batch's solves that has no tuned tile
  * shape yet, times one RK stage's pencil tiles of the whole batch for each
