@@ -340,7 +340,11 @@ def evaluate_leg(sg, stream, npts):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     nlev = len({tuple(r) for r in sg.index_map(Dv, kv, nv)[0]})
-    flops = npts * (nlev * kv ** (Dv - 1) * (2 * kv + 2 + Dv - 1) + Dv * (nv + 1) * 2 * kv * kv)
+    # FP64 operations per point (an FMA counts 2): per level block, with two
+    # dimensions contracted first (D >= 3), k^(D-2) (2k^2 + 2k + D), else
+    # k^(D-1) (2k + D + 1); plus the 1D basis tables
+    per_block = kv ** (Dv - 2) * (2 * kv * kv + 2 * kv + Dv) if Dv >= 3 else kv ** (Dv - 1) * (2 * kv + Dv + 1)
+    flops = npts * (nlev * per_block + Dv * (nv + 1) * 2 * kv * kv)
     t0 = time.perf_counter()
     vals = sg.reconstruct_DG(Dv, kv, nv, c, pts)
     e2e = time.perf_counter() - t0

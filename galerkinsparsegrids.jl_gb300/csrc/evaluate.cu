@@ -94,18 +94,43 @@ __global__ void __launch_bounds__(32 * kEvalWarps)
             }
             const double* c = coeffs + S.lev_off[t] + S.kD * cl;
             const double* v0 = tab + (L[0] - 1) * k;
-            // outer modes (m_1 .. m_{D-1}, m_1 fastest) times the inner sum over m_0
             int mo[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            const int64_t nout = S.kD / k;
-            for (int64_t o = 0; o < nout; o++) {
-                double prod = 1.0;
-                for (int d = 1; d < S.D; d++) prod *= tab[(d * nl + L[d] - 1) * k + mo[d]];
-                double s0 = 0.0;
-                for (int m0 = 0; m0 < k; m0++) s0 = fma(v0[m0], c[o * k + m0], s0);
-                acc = fma(prod, s0, acc);
-                for (int d = 1; d < S.D; d++) {  // next outer mode
-                    if (++mo[d] < k) break;
-                    mo[d] = 0;
+            if (S.D >= 3) {
+                // outer modes (m_2 .. m_{D-1}, m_2 fastest) times the sum over
+                // m_1 of v_1 times the inner sum over m_0: dimensions 0 and 1
+                // contracted before the outer product (k^(D-2) (k^2 + k + D - 2)
+                // FP64 operations per block instead of k^(D-1) (k + D - 1))
+                const double* v1 = tab + (nl + L[1] - 1) * k;
+                const int64_t nout = S.kD / (k * k);
+                for (int64_t o = 0; o < nout; o++) {
+                    double prod = 1.0;
+                    for (int d = 2; d < S.D; d++) prod *= tab[(d * nl + L[d] - 1) * k + mo[d]];
+                    const double* co = c + o * k * k;
+                    double s1 = 0.0;
+                    for (int m1 = 0; m1 < k; m1++) {
+                        double s0 = 0.0;
+                        for (int m0 = 0; m0 < k; m0++) s0 = fma(v0[m0], co[m1 * k + m0], s0);
+                        s1 = fma(v1[m1], s0, s1);
+                    }
+                    acc = fma(prod, s1, acc);
+                    for (int d = 2; d < S.D; d++) {  // next outer mode
+                        if (++mo[d] < k) break;
+                        mo[d] = 0;
+                    }
+                }
+            } else {
+                // outer modes (m_1 .. m_{D-1}, m_1 fastest) times the inner sum over m_0
+                const int64_t nout = S.kD / k;
+                for (int64_t o = 0; o < nout; o++) {
+                    double prod = 1.0;
+                    for (int d = 1; d < S.D; d++) prod *= tab[(d * nl + L[d] - 1) * k + mo[d]];
+                    double s0 = 0.0;
+                    for (int m0 = 0; m0 < k; m0++) s0 = fma(v0[m0], c[o * k + m0], s0);
+                    acc = fma(prod, s0, acc);
+                    for (int d = 1; d < S.D; d++) {  // next outer mode
+                        if (++mo[d] < k) break;
+                        mo[d] = 0;
+                    }
                 }
             }
         }
