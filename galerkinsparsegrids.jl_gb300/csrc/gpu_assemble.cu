@@ -154,7 +154,10 @@ std::vector<int64_t> scan_rows(const DevBuf& rowlen, int64_t m, cudaStream_t st)
     if (m) CK(cudaMemcpyAsync(h.data(), rowlen.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     std::vector<int64_t> rp(m + 1, 0);
-    for (int64_t r = 0; r < m; r++) rp[r + 1] = rp[r] + h[r];
+    for (int64_t r = 0; r < m; r++) {
+        if (h[r] < 0) throw Error(SGDG_ECUDA, "negative row length from a device count");
+        rp[r + 1] = rp[r] + h[r];
+    }
     return rp;
 }
 
@@ -257,6 +260,8 @@ std::unique_ptr<DeviceCSR> merge_terms(const std::vector<const DeviceCSR*>& term
 // the row comes out sorted.
 constexpr int kTLev = 16;         // levels per dimension (n + 1)
 constexpr int kTRowsPerBlock = 8;  // k_transform: one warp per row
+constexpr int64_t kTLongTuples = 1024;  // rows with this many level tuples or more: k_transform_long
+constexpr int kTLongThreads = 256;      // k_transform_long: one block per row
 
 struct TransArgs {
     int D, k, n, scheme, nlev;
@@ -367,12 +372,50 @@ __device__ int32_t tuple_entries(const TransArgs& A, const int* g, const int (*g
     return cnt;
 }
 
+// The level groups of row i's 1D row along dimension d (its nesting entries
+// grouped by level: [gs, ge) entries of level gl), ng[d] of them.
+__device__ void row_groups(const TransArgs& A, int64_t i, int d, int (*gs)[kTLev], int (*ge)[kTLev],
+                           int (*gl)[kTLev], int* ng) {
+    const int D = A.D, k = A.k;
+    int lo = 0, hi = A.nlev - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.lev_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const int8_t* Li = A.levels + (size_t)lo * D;
+    int64_t cl = (i - A.lev_off[lo]) / A.kD, ml = (i - A.lev_off[lo]) % A.kD;
+    int64_t i1 = 0;
+    for (int q = 0; q <= d; q++) {
+        const int L = Li[q];
+        const int64_t nc = (int64_t)1 << (L > 2 ? L - 2 : 0);
+        const int64_t c = cl % nc, m = ml % k;
+        cl /= nc;
+        ml /= k;
+        i1 = k * ((L >= 2 ? ((int64_t)1 << (L - 2)) : 0) + c) + m;
+    }
+    const int a = (int)A.rp1[i1], b = (int)A.rp1[i1 + 1];  // 1D transforms hold < 2^31 entries
+    int n = 0, last = -1;
+    for (int e = a; e < b; e++) {
+        int L, c, m;
+        dec1d(k, A.col1[e], L, c, m);
+        if (L != last) {
+            gs[d][n] = e;
+            gl[d][n] = L;
+            if (n > 0) ge[d][n - 1] = e;
+            n++;
+            last = L;
+        }
+    }
+    if (n > 0) ge[d][n - 1] = b;
+    ng[d] = n;
+}
+
 // One warp per row.  The row's level tuples (dimension 0 fastest, the order
 // of the global index) are taken 32 at a time, one per lane; a warp scan of
 // the lanes' entry counts places each lane's entries, so rounds and lanes
-// write the row in order.  Rows differ by four orders of magnitude in length
-// (a coarse modal row of n2m spans the whole grid), and the lanes split a long
-// row's tuples instead of one thread walking it.  The level groups of the
+// write the row in order.  Row lengths differ by four orders of magnitude (a
+// coarse modal row of n2m spans the whole grid): rows of kTLongTuples level
+// tuples or more are left to k_transform_long.  The level groups of the
 // row's 1D rows (one lane per dimension builds them) live in shared memory,
 // one copy per warp.
 template <bool FILL>
@@ -384,50 +427,19 @@ __global__ void __launch_bounds__(32 * kTRowsPerBlock)
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t i = (int64_t)blockIdx.x * kTRowsPerBlock + wib;
     if (i >= A.N) return;  // the whole warp
-    const int D = A.D, k = A.k;
+    const int D = A.D;
     int(*gs)[kTLev] = s_grp[wib][0];
     int(*ge)[kTLev] = s_grp[wib][1];
     int(*gl)[kTLev] = s_grp[wib][2];
     int* ng = s_ng[wib];
-    if (lane < D) {
-        // (level, cell, mode) of row i along dimension `lane` -> its 1D row
-        int lo = 0, hi = A.nlev - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (A.lev_off[mid] <= i) lo = mid; else hi = mid - 1;
-        }
-        const int8_t* Li = A.levels + (size_t)lo * D;
-        int64_t cl = (i - A.lev_off[lo]) / A.kD, ml = (i - A.lev_off[lo]) % A.kD;
-        int64_t i1 = 0;
-        for (int d = 0; d <= lane; d++) {
-            const int L = Li[d];
-            const int64_t nc = (int64_t)1 << (L > 2 ? L - 2 : 0);
-            const int64_t c = cl % nc, m = ml % k;
-            cl /= nc;
-            ml /= k;
-            i1 = k * ((L >= 2 ? ((int64_t)1 << (L - 2)) : 0) + c) + m;
-        }
-        const int a = (int)A.rp1[i1], b = (int)A.rp1[i1 + 1];  // 1D transforms hold < 2^31 entries
-        // level groups of the 1D row: [gs, ge) entries of level gl
-        int n = 0, last = -1;
-        for (int e = a; e < b; e++) {
-            int L, c, m;
-            dec1d(k, A.col1[e], L, c, m);
-            if (L != last) {
-                gs[lane][n] = e;
-                gl[lane][n] = L;
-                if (n > 0) ge[lane][n - 1] = e;
-                n++;
-                last = L;
-            }
-        }
-        if (n > 0) ge[lane][n - 1] = b;
-        ng[lane] = n;
-    }
+    if (lane < D) row_groups(A, i, lane, gs, ge, gl, ng);
     __syncwarp();
     int64_t ntup = 1;
     for (int d = 0; d < D; d++) ntup *= ng[d];
-    if (ntup == 0) {  // an empty 1D row: no entries in row i
+    // an empty 1D row: no entries in row i; a long row: k_transform_long,
+    // launched after this kernel, overwrites the 0 (every row's count is
+    // written here, so no row pointer comes from an unwritten count)
+    if (ntup == 0 || ntup >= kTLongTuples) {
         if (!FILL && lane == 0) rowlen[i] = 0;
         return;  // the whole warp
     }
@@ -456,6 +468,61 @@ __global__ void __launch_bounds__(32 * kTRowsPerBlock)
         w += rsum;
     }
     if (!FILL && lane == 0) rowlen[i] = (int32_t)w;
+}
+
+// The rows with kTLongTuples level tuples or more, one block of
+// kTLongThreads per row: the same walk as k_transform with the tuples taken
+// kTLongThreads at a time and a block scan of the counts.
+template <bool FILL>
+__global__ void __launch_bounds__(kTLongThreads)
+    k_transform_long(TransArgs A, const int32_t* __restrict__ rows, int32_t* rowlen,
+                     const int64_t* __restrict__ rowptr, int32_t* __restrict__ col, double* __restrict__ val) {
+    __shared__ int s_grp[3][8][kTLev];
+    __shared__ int s_ng[8];
+    __shared__ int32_t s_warp[kTLongThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int64_t i = rows[blockIdx.x];
+    const int D = A.D;
+    int(*gs)[kTLev] = s_grp[0];
+    int(*ge)[kTLev] = s_grp[1];
+    int(*gl)[kTLev] = s_grp[2];
+    if (tid < D) row_groups(A, i, tid, gs, ge, gl, s_ng);
+    __syncthreads();
+    int64_t ntup = 1;
+    for (int d = 0; d < D; d++) ntup *= s_ng[d];
+    int64_t w = FILL ? rowptr[i] : 0;
+    const int64_t lim = FILL ? rowptr[i + 1] : 0;
+    for (int64_t t0 = 0; t0 < ntup; t0 += kTLongThreads) {  // ntup is the same in every thread
+        const int64_t t = t0 + tid;
+        int g[8];
+        int32_t c = 0;
+        if (t < ntup) {
+            int64_t r = t;
+            for (int d = 0; d < D; d++) {
+                g[d] = (int)(r % s_ng[d]);
+                r /= s_ng[d];
+            }
+            c = tuple_entries<false>(A, g, gs, ge, gl, 0, 0, nullptr, nullptr);
+        }
+        int32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_warp[wid] = incl;
+        __syncthreads();
+        int32_t before = 0, total = 0;
+        for (int q = 0; q < kTLongThreads / 32; q++) {
+            const int32_t x = s_warp[q];
+            if (q < wid) before += x;
+            total += x;
+        }
+        if (FILL && c > 0) tuple_entries<true>(A, g, gs, ge, gl, w + before + incl - c, lim, col, val);
+        w += total;
+        __syncthreads();  // s_warp is rewritten next round
+    }
+    if (!FILL && tid == 0) rowlen[i] = (int32_t)w;
 }
 
 }  // namespace
@@ -506,10 +573,51 @@ std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, c
            d_cl = upload(cl, st), d_vl = upload(vl, st);
     TransArgs A{D, k, n, ix.scheme, ix.nlev, ix.N, ix.kD, d_lv.as<int8_t>(), d_lo.as<int32_t>(), d_code.as<int32_t>(),
                 d_rp.as<int64_t>(), d_cl.as<int32_t>(), d_vl.as<double>()};
+    // rows with kTLongTuples level tuples or more (the product over the
+    // dimensions of the levels present in each 1D row, as the kernels count
+    // them) go to k_transform_long
+    std::vector<int> nlev1(T1.m, 0);
+    for (int64_t r = 0; r < T1.m; r++) {
+        int last = -1;
+        for (int64_t p = rp[r]; p < rp[r + 1]; p++) {
+            const int blk = cl[p] / k;
+            int L = 1;
+            while (L < 32 && (blk >> (L - 1)) != 0) L++;
+            if (L != last) nlev1[r]++;
+            last = L;
+        }
+    }
+    std::vector<int32_t> long_rows;
+    for (int b = 0; b < ix.nlev; b++) {
+        const int* L = &ix.levels[(size_t)b * D];
+        int64_t nc[8], cells = 1;
+        for (int d = 0; d < D; d++) {
+            nc[d] = ncells(L[d]);
+            cells *= nc[d];
+        }
+        for (int64_t c = 0; c < cells; c++)
+            for (int64_t m = 0; m < ix.kD; m++) {
+                int64_t cr = c, mr = m, ntup = 1;
+                for (int d = 0; d < D; d++) {
+                    const int64_t i1 = k * ((L[d] >= 2 ? ((int64_t)1 << (L[d] - 2)) : 0) + cr % nc[d]) + mr % k;
+                    cr /= nc[d];
+                    mr /= k;
+                    ntup *= nlev1[(size_t)i1];
+                }
+                if (ntup >= kTLongTuples) long_rows.push_back((int32_t)(ix.lev_off[b] + c * ix.kD + m));
+            }
+    }
+    DevBuf d_long = upload(long_rows, st);
+    const int nlong = (int)long_rows.size();
     DevBuf rowlen(sizeof(int32_t) * (size_t)ix.N);
     const int tgrid = (int)((ix.N + kTRowsPerBlock - 1) / kTRowsPerBlock);
     k_transform<false><<<tgrid, 32 * kTRowsPerBlock, 0, st>>>(A, rowlen.as<int32_t>(), nullptr, nullptr, nullptr);
     CK(cudaGetLastError());
+    if (nlong > 0) {
+        k_transform_long<false><<<nlong, kTLongThreads, 0, st>>>(A, d_long.as<int32_t>(), rowlen.as<int32_t>(), nullptr,
+                                                                 nullptr, nullptr);
+        CK(cudaGetLastError());
+    }
     std::vector<int64_t> rph = scan_rows(rowlen, ix.N, st);
     auto R = std::make_unique<DeviceCSR>();
     R->rowptr = upload(rph, st);
@@ -518,6 +626,12 @@ std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, c
     k_transform<true><<<tgrid, 32 * kTRowsPerBlock, 0, st>>>(A, nullptr, R->rowptr.as<int64_t>(),
                                                               R->col.as<int32_t>(), R->val.as<double>());
     CK(cudaGetLastError());
+    if (nlong > 0) {
+        k_transform_long<true><<<nlong, kTLongThreads, 0, st>>>(A, d_long.as<int32_t>(), nullptr,
+                                                                R->rowptr.as<int64_t>(), R->col.as<int32_t>(),
+                                                                R->val.as<double>());
+        CK(cudaGetLastError());
+    }
     CK(cudaStreamSynchronize(st));
     finish_device_csr(*R, rph, ix.N, st);
     return R;

@@ -44,9 +44,12 @@ WHICH = [("modal", "nodal"), ("nodal", "points"), ("points", "nodal"), ("nodal",
 
 
 @pytest.mark.gpu
+# (6, 2, 3): the coarse modal rows of n2m and m2n have 4^6 = 4096 level
+# tuples, above the 1,024 from which a row gets a whole block
+# (k_transform_long); the other cases stay in the warp-per-row kernel
 @pytest.mark.parametrize("D,k,n,scheme", [(1, 3, 4, "sparse"), (2, 2, 3, "sparse"), (2, 3, 4, "sparse"),
                                           (3, 2, 3, "sparse"), (4, 2, 3, "sparse"), (2, 5, 3, "sparse"),
-                                          (2, 2, 3, "full")])
+                                          (2, 2, 3, "full"), (6, 2, 3, "sparse")])
 def test_device_transforms_equal_host(sgdg, D, k, n, scheme):
     # the restricted Kronecker products (src/multidim_nodal_basis.jl:40-109)
     for w in WHICH:
