@@ -7,13 +7,13 @@
 // the transpose-order of the reference's CSC build and yields the same set of
 // stored entries (numerical zeros included).
 //
-// Sums and products keep the structural pattern.  The reference's
-// laplacian_matrix (src/multidim_derivative.jl:71-79) adds with
-// SparseArrays' map(+), which also drops entries whose floating-point sum is
-// exactly 0.0; which entries cancel exactly depends on the roundoff of its
-// quadrature, so that subset cannot be reproduced by any other
-// implementation.  The structural pattern stored here is a superset of it;
-// the extra entries hold values at roundoff level.
+// Products keep their structural pattern (SparseArrays' spmatmul stores every
+// structural entry).  Sums follow SparseArrays' map(+): an entry present in
+// only one operand is added to 0.0, and every result that is exactly 0.0 is
+// dropped -- the reference's laplacian_matrix (src/multidim_derivative.jl:
+// 71-79) and the advection sum of the D_d lose the entries whose products
+// cancel exactly.  The 1D operator is built by the reference's route
+// (dlf1d.cpp), so the same sums cancel here.
 #include <algorithm>
 #include <cstring>
 
@@ -102,7 +102,8 @@ CSR assemble_dd(const SparseIndex& ix, const DLF1D& op, int d) {
     return A;
 }
 
-// sum_i A_i * A_i, structural pattern
+// sum_i A_i * A_i: each product with its structural pattern, summed with
+// map(+)'s exact-zero drop
 CSR spgemm_sum(const std::vector<const CSR*>& As) {
     const int64_t N = As[0]->m;
     CSR out;
@@ -160,16 +161,22 @@ CSR spgemm_sum(const std::vector<const CSR*>& As) {
             }
             cur.swap(merged);
         }
-        out.rowptr[i + 1] = out.rowptr[i] + (int64_t)cur.size();
+        // a sum that cancels to exactly 0.0 is not stored (dropping it after
+        // the last term leaves the same entries and values as dropping after
+        // every term: 0.0 + x == x)
+        int64_t kept = 0;
         for (auto& e : cur) {
+            if (e.second == 0.0) continue;
             out.col.push_back(e.first);
             out.val.push_back(e.second);
+            kept++;
         }
+        out.rowptr[i + 1] = out.rowptr[i] + kept;
     }
     return out;
 }
 
-// sum_i s_i A_i over the union of patterns
+// sum_i s_i A_i over the union of patterns, exact zeros dropped
 CSR add_scaled(const std::vector<const CSR*>& As, const std::vector<double>& s) {
     const int64_t N = As[0]->m;
     CSR out;
@@ -206,11 +213,17 @@ CSR add_scaled(const std::vector<const CSR*>& As, const std::vector<double>& s) 
             }
             cur.swap(merged);
         }
-        out.rowptr[i + 1] = out.rowptr[i] + (int64_t)cur.size();
+        // a sum that cancels to exactly 0.0 is not stored (dropping it after
+        // the last term leaves the same entries and values as dropping after
+        // every term: 0.0 + x == x)
+        int64_t kept = 0;
         for (auto& e : cur) {
+            if (e.second == 0.0) continue;
             out.col.push_back(e.first);
             out.val.push_back(e.second);
+            kept++;
         }
+        out.rowptr[i + 1] = out.rowptr[i] + kept;
     }
     return out;
 }

@@ -1,22 +1,25 @@
 // dlf1d.cpp -- the 1D hierarchical periodic DG derivative with central flux.
 //
-// The reference builds it in the finest position basis and conjugates
-// (src/1d_derivative.jl:108-117: hier2pos' * (-D + LF)' * hier2pos).  Because
-// hier2pos is an exact change of orthonormal basis, the same operator is,
-// entry by entry in the hierarchical basis,
-//     D[h', h] = - int v_h (d/dx v_h') dx  -  sum_e avg(v_h)(e) [[v_h']](e),
-// where e runs over the points where the row function v_h' jumps (its support
-// ends and midpoint, or the periodic point 0 = 1 at level 0), avg is the mean
-// of the two one-sided limits (alpha = 0 flux, src/1d_derivative.jl:66-67) and
-// [[g]](e) = g(e+) - g(e-).  This file evaluates that formula with exact
-// one-sided limits and Gauss-Legendre quadrature (exact for these piecewise
-// polynomials), so values agree with the reference to roundoff (the reference
-// evaluates edges at +-5e-16, src/1d_derivative.jl:56-64, which moves its
-// entries by ~1e-13 relative).
+// Built by the reference's own route, step by step in its arithmetic order,
+// so that the stored pattern and the values are the ones the reference's
+// sparse algebra produces:
+//   Q  = hier2pos(k, n)                      src/1d_dg_functions.jl:242-263
+//   A  = (-D_matrix(k, n) + periodic_LF_matrix(k, n))'
+//                                            src/1d_derivative.jl:21-111
+//   op = Q' * (A * Q)                        src/1d_derivative.jl:113-117
+// The sums of the derivative matrix keep exactly the entries whose floating-
+// point sums do not cancel to 0.0 (SparseArrays' map(+) drops exact zeros),
+// and which sums cancel depends on every rounding before them; so the basis
+// evaluation (Horner on the x^i / sgn(x) x^i coefficient pairs), the cell-edge
+// evaluation at +-5e-16, the SpGEMM accumulation order (terms in increasing
+// inner index, the first one assigned) and the exact-zero drops all follow
+// the reference.  hquadrature (HCubature 1.4.0, atol 1e-12) integrates
+// piecewise polynomials of degree <= 2k-2 here; it is restated as a 16-point
+// Gauss-Legendre rule per finest cell, exact for these integrands.
 //
-// Stored pattern: a dense k x k block for every pair of (level, cell) blocks
-// whose closed supports meet periodically -- the structural pattern the
-// reference's two SpGEMMs leave for n >= 2 (numerical zeros included).
+// The result is block-dense: one full k x k block for every pair of (level,
+// cell) blocks whose closed supports meet periodically (numerical zeros
+// included); build_dlf checks that and stores it block by block.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -27,42 +30,297 @@
 namespace sgdg {
 namespace {
 
+constexpr double kEdge = 5.0e-16;  // src/1d_derivative.jl:56
+constexpr int kLegHalf = kKMax + 1;  // leg_coeffs vectors hold 2 (K_max + 1) numbers
+
+// Gauss-Legendre nodes and weights on [-1, 1]: Newton's method on the
+// three-term recurrence from the Chebyshev-like guess, stopping once a step
+// moves the node by less than 1e-16.
 void gauss_legendre(int q, std::vector<double>& x, std::vector<double>& w) {
     x.assign(q, 0.0);
     w.assign(q, 0.0);
     for (int i = 0; i < (q + 1) / 2; i++) {
-        double z = std::cos(M_PI * (i + 0.75) / (q + 0.5)), dp = 1.0;
+        double z = std::cos(M_PI * (i + 0.75) / (q + 0.5)), slope = 0.0;
         for (int it = 0; it < 100; it++) {
-            double p0 = 1.0, p1 = z;
-            for (int j = 2; j <= q; j++) {
-                double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
-                p0 = p1;
-                p1 = p2;
+            double pj = 1.0, pjm1 = 0.0;
+            for (int j = 1; j <= q; j++) {
+                const double pjm2 = pjm1;
+                pjm1 = pj;
+                pj = ((2.0 * j - 1.0) * z * pjm1 - (j - 1.0) * pjm2) / j;
             }
-            if (q == 1) {
-                p1 = z;
-                p0 = 1.0;
-            }
-            dp = q * (z * p1 - p0) / (z * z - 1.0);
-            double dz = p1 / dp;
-            z -= dz;
-            if (std::fabs(dz) < 1e-17) break;
+            slope = q * (z * pj - pjm1) / (z * z - 1.0);
+            const double prev = z;
+            z = prev - pj / slope;
+            if (std::fabs(z - prev) < 1e-16) break;
         }
         x[i] = -z;
         x[q - 1 - i] = z;
-        w[i] = w[q - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+        w[i] = w[q - 1 - i] = 2.0 / ((1.0 - z * z) * slope * slope);
     }
 }
 
-bool touch(double a0, double a1, double b0, double b1) {
-    if (a0 <= b1 && b0 <= a1) return true;
-    return (a0 == 0.0 && b1 == 1.0) || (b0 == 0.0 && a1 == 1.0);
+// array2poly (src/1d_dg_functions.jl:15-27): coefficients of x^i (first half)
+// and sgn(x) x^i (second half) of a polynomial piece on [-1, 1], zero outside
+double array2poly(const double* c, int half, double x) {
+    if (std::fabs(x) > 1) return 0.0;
+    double s = 0.0;
+    for (int i = half - 1; i >= 0; i--) {
+        s = s * x;
+        s = s + (c[i] + (std::signbit(x) ? -c[i + half] : c[i + half]));
+    }
+    return s;
 }
 
-void block_support(int L, int c, double& x0, double& x1) {
-    double w = 1.0 / double(ncells(L));
-    x0 = (c - 1) * w;
-    x1 = c * w;
+// product_matrix (src/dg_basis.jl:21-35): <x^i, x^j> on [-1, 1] with the
+// reflected halves, exact rationals evaluated in floating point
+int sign_pow(int e) { return e % 2 == 0 ? 1 : -1; }
+double product_matrix(int i, int j, int n) {
+    const int h = n / 2;
+    if (i < h && j < h) return (double)(1 + sign_pow(i + j)) / (double)(1 + i + j);
+    if (i >= h && j < h) return (double)(1 - sign_pow((i - h) + j)) / (double)(1 + (i - h) + j);
+    if (i < h && j >= h) return product_matrix(j, i, n);
+    return (double)(1 + sign_pow((i - h) + (j - h))) / (double)(1 + (i - h) + (j - h));
+}
+
+// inner_product (src/dg_basis.jl:37-50)
+double inner_product(const double* a, const double* b, int n) {
+    double value = 0.0;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            if (a[i] == 0 || b[j] == 0) continue;
+            value += product_matrix(i, j, n) * a[i] * b[j];
+        }
+    return value;
+}
+
+// The reference's basis functions on [0, 1] from the coefficient arrays.
+struct RefBasis {
+    int k = 0;
+    std::vector<double> leg;  // (K_max + 1) arrays of 2 (K_max + 1): normalised Legendre P_m
+    const double* dg = nullptr;  // k arrays of 2k: the multiwavelets h_mode
+
+    explicit RefBasis(int k_) : k(k_) {
+        const Basis1D& B = basis(k_);
+        dg = B.dg.data();
+        leg.assign((size_t)(kKMax + 1) * 2 * kLegHalf, 0.0);
+        for (int m = 0; m <= kKMax; m++)
+            for (int t = 0; t <= kKMax; t++) leg[(size_t)m * 2 * kLegHalf + t] = B.leg[(size_t)m * (kKMax + 1) + t];
+    }
+    const double* legendre(int m) const { return &leg[(size_t)m * 2 * kLegHalf]; }
+    // LegendreP (src/1d_dg_functions.jl:34-44)
+    double P(int m, double x) const { return array2poly(legendre(m), kLegHalf, x); }
+    // v (src/dg_methods.jl:27-36): hierarchical function of 0-based level
+    double v(int level, int cell, int mode, double x) const {
+        if (level == 0) return P(mode - 1, 2 * x - 1) * std::sqrt(2.0);
+        return array2poly(dg + (size_t)(mode - 1) * 2 * k, k, (double)(int64_t(1) << level) * x - (double)(2 * cell - 1)) *
+               std::sqrt(1.0 * (double)(int64_t(1) << level));
+    }
+    // leg and basis (src/1d_dg_functions.jl:83-97): position basis of a level
+    double leg01(int mode, double x) const { return std::sqrt(2.0) * P(mode - 1, 2 * x - 1); }
+    double pos(int level, int cell, int mode, double x) const {
+        return leg01(mode, (double)(int64_t(1) << level) * x - (double)(cell - 1)) * std::pow(2.0, (double)level / 2.0);
+    }
+};
+
+// Row-compressed sparse matrix for the reference's sparse algebra.  Rows
+// are kept sorted; "sum" steps drop results that are exactly 0.0.
+struct Sp {
+    int64_t m = 0, n = 0;
+    std::vector<int64_t> rp;
+    std::vector<int32_t> ci;
+    std::vector<double> v;
+    explicit Sp(int64_t m_ = 0, int64_t n_ = 0) : m(m_), n(n_), rp(m_ + 1, 0) {}
+    void push(int32_t c, double x) {
+        ci.push_back(c);
+        v.push_back(x);
+    }
+    void end_row(int64_t r) { rp[r + 1] = (int64_t)ci.size(); }
+};
+
+Sp transpose(const Sp& A) {
+    Sp T(A.n, A.m);
+    std::vector<int64_t> cnt(A.n + 1, 0);
+    for (int32_t c : A.ci) cnt[c + 1]++;
+    for (int64_t c = 0; c < A.n; c++) cnt[c + 1] += cnt[c];
+    T.rp = cnt;
+    T.ci.resize(A.ci.size());
+    T.v.resize(A.v.size());
+    for (int64_t r = 0; r < A.m; r++)
+        for (int64_t p = A.rp[r]; p < A.rp[r + 1]; p++) {
+            const int64_t q = cnt[A.ci[p]]++;
+            T.ci[q] = (int32_t)r;
+            T.v[q] = A.v[p];
+        }
+    return T;
+}
+
+// A * B, Gustavson by rows: C[r, c] accumulates A[r, j] * B[j, c] over the
+// stored j of row r in increasing order, the first product assigned (the
+// order of SparseArrays' column-by-column spmatmul); structural zeros kept.
+Sp spgemm(const Sp& A, const Sp& B) {
+    Sp C(A.m, B.n);
+    std::vector<int64_t> mark(B.n, -1);
+    std::vector<double> acc(B.n, 0.0);
+    std::vector<int32_t> cols;
+    for (int64_t r = 0; r < A.m; r++) {
+        cols.clear();
+        for (int64_t p = A.rp[r]; p < A.rp[r + 1]; p++) {
+            const int32_t j = A.ci[p];
+            const double a = A.v[p];
+            for (int64_t q = B.rp[j]; q < B.rp[j + 1]; q++) {
+                const int32_t c = B.ci[q];
+                if (mark[c] != r) {
+                    mark[c] = r;
+                    acc[c] = a * B.v[q];
+                    cols.push_back(c);
+                } else {
+                    acc[c] += a * B.v[q];
+                }
+            }
+        }
+        std::sort(cols.begin(), cols.end());
+        for (int32_t c : cols) C.push(c, acc[c]);
+        C.end_row(r);
+    }
+    return C;
+}
+
+// -A + B over the union of the patterns, results that are exactly zero dropped
+// (SparseArrays' unary minus, then map(+); a missing operand is 0.0)
+Sp neg_plus(const Sp& A, const Sp& B) {
+    Sp C(A.m, A.n);
+    for (int64_t r = 0; r < A.m; r++) {
+        int64_t a = A.rp[r], b = B.rp[r];
+        const int64_t ae = A.rp[r + 1], be = B.rp[r + 1];
+        while (a < ae || b < be) {
+            const int32_t ca = a < ae ? A.ci[a] : INT32_MAX, cb = b < be ? B.ci[b] : INT32_MAX;
+            double x;
+            int32_t c;
+            if (ca == cb) {
+                x = -1.0 * A.v[a++] + 1.0 * B.v[b++];
+                c = ca;
+            } else if (ca < cb) {
+                x = -1.0 * A.v[a++] + 0.0;
+                c = ca;
+            } else {
+                x = 0.0 + 1.0 * B.v[b++];
+                c = cb;
+            }
+            if (x != 0) C.push(c, x);
+        }
+        C.end_row(r);
+    }
+    return C;
+}
+
+// hier2pos (src/1d_dg_functions.jl:242-263): Q[pos(cell, p), hier(level, cell', mode)]
+// = <v_hier, basis_pos> over each finest cell, kept when |value| > 1e-12.
+// Cells outside a hierarchical function's support contribute exact zeros
+// (the function is 0.0 at every node there) and are not visited.
+Sp hier2pos(const RefBasis& B, int n) {
+    const int k = B.k;
+    const int64_t len = (int64_t)k << n;
+    std::vector<double> gx, gw;
+    gauss_legendre(16, gx, gw);
+    const double hcell = 1.0 / (double)(int64_t(1) << n);
+    Sp Qt(len, len);  // built by hierarchical column, transposed at the end
+    int64_t j = 0;
+    for (int level = 0; level <= n; level++) {
+        const int ncell = 1 << (level > 1 ? level - 1 : 0);
+        for (int cell = 1; cell <= ncell; cell++)
+            for (int mode = 1; mode <= k; mode++) {
+                const int span = level == 0 ? 1 << n : 1 << (n - level + 1);
+                const int i0 = level == 0 ? 1 : (cell - 1) * span + 1;
+                for (int i = i0; i < i0 + span; i++) {
+                    const double a = (double)(i - 1) * hcell, b = (double)i * hcell;
+                    for (int p = 1; p <= k; p++) {
+                        double s = 0.0;
+                        for (int t = 0; t < 16; t++) {
+                            const double x = 0.5 * (a + b) + 0.5 * (b - a) * gx[t];
+                            s += gw[t] * B.v(level, cell, mode, x) * B.pos(n, i, p, x);
+                        }
+                        s *= 0.5 * (b - a);
+                        if (std::fabs(s) > 1e-12) Qt.push((int32_t)((int64_t)(i - 1) * k + (p - 1)), s);
+                    }
+                }
+                Qt.end_row(j);
+                j++;
+            }
+    }
+    return transpose(Qt);
+}
+
+// symbolic_diff (src/derivative_matrix_elements.jl:80-94) and
+// legendreDlegendre (src/derivative_matrix_elements.jl:101-103)
+double legendre_d_legendre(const RefBasis& B, int m1, int m2) {
+    const int n = 2 * kLegHalf, h = kLegHalf;
+    const double* v = B.legendre(m2 - 1);
+    std::vector<double> d(n, 0.0);
+    for (int i = 1; i <= n; i++) {
+        if (i < h)
+            d[i - 1] = (double)i * v[i];
+        else if (i > h && i < 2 * h)
+            d[i - 1] = (double)(i - h) * v[i];
+    }
+    return inner_product(B.legendre(m1 - 1), d.data(), n);
+}
+
+// D_matrix(k, level) (src/1d_derivative.jl:21-44, legvDv at
+// src/derivative_matrix_elements.jl:106-112): cell-diagonal, |val| > 1e-15
+Sp pos_derivative(const RefBasis& B, int level) {
+    const int k = B.k, ncell = 1 << level;
+    Sp D((int64_t)k << level, (int64_t)k << level);
+    std::vector<double> lDl((size_t)k * k);
+    for (int m1 = 1; m1 <= k; m1++)
+        for (int m2 = 1; m2 <= k; m2++) lDl[(m1 - 1) * k + (m2 - 1)] = legendre_d_legendre(B, m1, m2);
+    for (int cell = 1; cell <= ncell; cell++)
+        for (int m1 = 1; m1 <= k; m1++) {
+            for (int m2 = 1; m2 <= k; m2++) {
+                const double val = (double)(int64_t(1) << (level + 1)) * lDl[(m1 - 1) * k + (m2 - 1)];
+                if (std::fabs(val) > 1.0e-15) D.push((int32_t)((cell - 1) * k + (m2 - 1)), val);
+            }
+            D.end_row((int64_t)(cell - 1) * k + (m1 - 1));
+        }
+    return D;
+}
+
+// periodic_legvLFv (src/1d_derivative.jl:52-74, alpha = 0)
+double periodic_lf_entry(const RefBasis& B, int level, int cell1, int mode1, int cell2, int mode2) {
+    const double N = (double)(int64_t(1) << level);
+    const double point1 = (double)(cell2 - 1) / N, point2 = (double)cell2 / N;
+    double left1 = B.pos(level, cell1, mode1, point1 - kEdge);
+    const double right1 = B.pos(level, cell1, mode1, point1 + kEdge);
+    const double left2 = B.pos(level, cell1, mode1, point2 - kEdge);
+    double right2 = B.pos(level, cell1, mode1, point2 + kEdge);
+    if (cell2 == (1 << level)) right2 = B.pos(level, cell1, mode1, 0.0 + kEdge);
+    if (cell2 == 1) left1 = B.pos(level, cell1, mode1, 1.0 - kEdge);
+    const double LF1 = 0.5 * (left1 + right1) + 0.0 * (right1 - left1);
+    const double LF2 = 0.5 * (left2 + right2) + 0.0 * (right2 - left2);
+    const double val1 = B.pos(level, cell2, mode2, point1 + kEdge);
+    const double val2 = B.pos(level, cell2, mode2, point2 - kEdge);
+    return LF2 * val2 - LF1 * val1;
+}
+
+// periodic_LF_matrix (src/1d_derivative.jl:76-100), |val| > 1e-15.  The
+// flux couples a cell only to itself and its periodic neighbours (basis()
+// is 0.0 at every evaluation point of any other pair), so only those pairs
+// are evaluated.
+Sp periodic_lf(const RefBasis& B, int level) {
+    const int k = B.k, ncell = 1 << level;
+    Sp L((int64_t)k << level, (int64_t)k << level);
+    for (int cell1 = 1; cell1 <= ncell; cell1++)
+        for (int mode1 = 1; mode1 <= k; mode1++) {
+            for (int cell2 = 1; cell2 <= ncell; cell2++) {
+                const int dc = (cell2 - cell1 + ncell) % ncell;
+                if (!(dc == 0 || dc == 1 || dc == ncell - 1)) continue;
+                for (int mode2 = 1; mode2 <= k; mode2++) {
+                    const double val = periodic_lf_entry(B, level, cell1, mode1, cell2, mode2);
+                    if (std::fabs(val) > 1.0e-15) L.push((int32_t)((cell2 - 1) * k + (mode2 - 1)), val);
+                }
+            }
+            L.end_row((int64_t)(cell1 - 1) * k + (mode1 - 1));
+        }
+    return L;
 }
 
 }  // namespace
@@ -70,6 +328,10 @@ void block_support(int L, int c, double& x0, double& x1) {
 static DLF1D build_dlf(int k, int n) {
     if (n < 2) throw Error(1, "n must be >= 2 (with <= 2 finest cells the reference's periodic fluxes cancel)");
     if (n > 20) throw Error(1, "n too large");
+    const RefBasis B(k);
+    const Sp Q = hier2pos(B, n);
+    const Sp A = transpose(neg_plus(pos_derivative(B, n), periodic_lf(B, n)));  // periodic_pos_DLF_matrix
+    const Sp R = spgemm(transpose(Q), spgemm(A, Q));                              // periodic_hier_DLF_matrix
     DLF1D op;
     op.k = k;
     op.n = n;
@@ -79,63 +341,26 @@ static DLF1D build_dlf(int k, int n) {
             op.blk_level.push_back(L);
             op.blk_cell.push_back(c);
         }
-    std::vector<double> gx, gw;
-    gauss_legendre(k + 1, gx, gw);
-    // hierarchical functions per block
-    std::vector<std::vector<HierFn>> fns(op.nblocks);
-    for (int b = 0; b < op.nblocks; b++)
-        for (int m = 1; m <= k; m++) fns[b].push_back(make_hier_fn(k, op.blk_level[b] - 1, op.blk_cell[b], m));
+    // block-CSR over (level, cell) blocks: every row of a row block must
+    // list the same column blocks with all k modes
     op.rowptr.assign(op.nblocks + 1, 0);
     for (int rb = 0; rb < op.nblocks; rb++) {
-        double r0, r1;
-        block_support(op.blk_level[rb], op.blk_cell[rb], r0, r1);
-        const auto& row = fns[rb];
-        // jump points of the row functions, taken mod 1 (0 and 1 are one point)
-        std::vector<double> E;
-        if (row[0].level == 0)
-            E = {0.0};
-        else
-            for (double e : {row[0].x0, row[0].xm, row[0].x1}) {
-                double em = e >= 1.0 ? e - 1.0 : e;
-                if (std::find(E.begin(), E.end(), em) == E.end()) E.push_back(em);
+        const int64_t r0 = (int64_t)rb * k;
+        const int64_t len = R.rp[r0 + 1] - R.rp[r0];
+        if (len % k != 0) throw Error(7, "1D operator: a row is not block-dense");
+        const size_t first = op.val.size();
+        op.val.resize(first + (size_t)(len / k) * k * k);
+        for (int64_t b = 0; b < len / k; b++) op.colblk.push_back(R.ci[R.rp[r0] + b * k] / k);
+        for (int i = 0; i < k; i++) {
+            const int64_t p0 = R.rp[r0 + i];
+            if (R.rp[r0 + i + 1] - p0 != len) throw Error(7, "1D operator: a row block is not block-dense");
+            for (int64_t t = 0; t < len; t++) {
+                const int64_t b = t / k;
+                const int32_t c = R.ci[p0 + t];
+                if (c != op.colblk[op.colblk.size() - len / k + b] * k + (int32_t)(t % k))
+                    throw Error(7, "1D operator: a row block is not block-dense");
+                op.val[first + (size_t)b * k * k + (size_t)i * k + (size_t)(t % k)] = R.v[p0 + t];
             }
-        for (int cb = 0; cb < op.nblocks; cb++) {
-            double c0, c1;
-            block_support(op.blk_level[cb], op.blk_cell[cb], c0, c1);
-            if (!touch(r0, r1, c0, c1)) continue;
-            const auto& col = fns[cb];
-            // volume-term intervals: intersection split at both midpoints
-            double lo = std::max(r0, c0), hi = std::min(r1, c1);
-            std::vector<double> bp;
-            if (lo < hi) {
-                bp = {lo, hi};
-                for (double p : {row[0].xm, col[0].xm})
-                    if (p > lo && p < hi) bp.push_back(p);
-                std::sort(bp.begin(), bp.end());
-            }
-            for (int i = 0; i < k; i++)
-                for (int j = 0; j < k; j++) {
-                    const HierFn& fr = row[i];
-                    const HierFn& fc = col[j];
-                    double vol = 0.0;
-                    for (size_t s = 0; s + 1 < bp.size(); s++) {
-                        double a = bp[s], b = bp[s + 1], hh = 0.5 * (b - a), mid = 0.5 * (a + b);
-                        double acc = 0.0;
-                        for (size_t t = 0; t < gx.size(); t++) {
-                            double x = mid + hh * gx[t];
-                            acc += gw[t] * hier_value(fc, x, +1) * hier_deriv(fr, x, +1);
-                        }
-                        vol += acc * hh;
-                    }
-                    double flux = 0.0;
-                    for (double e : E) {
-                        double avg = 0.5 * (hier_value(fc, e, -1) + hier_value(fc, e, +1));
-                        double jump = hier_value(fr, e, +1) - hier_value(fr, e, -1);
-                        flux += avg * jump;
-                    }
-                    op.val.push_back(-vol - flux);
-                }
-            op.colblk.push_back(cb);
         }
         op.rowptr[rb + 1] = (int32_t)op.colblk.size();
     }

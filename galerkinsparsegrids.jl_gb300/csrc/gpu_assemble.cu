@@ -12,8 +12,9 @@
 // row, and after a host prefix sum of the counts writes the row, columns in
 // ascending order.  Sums over d merge the D sorted rows with the fold the
 // host's spgemm_sum / add_scaled use (0.0 + term_0 + term_1 + ..., a missing
-// term being 0.0, products rounded before the add), so the device operator
-// holds the same stored entries and the same values as the host one.
+// term being 0.0, products rounded before the add) and drop sums that are
+// exactly 0.0, so the device operator holds the same stored entries and the
+// same values as the host one.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -101,7 +102,8 @@ struct SumArgs {
     int scaled;
 };
 
-// merge of the terms' sorted rows: count (rowlen) or write (col, val)
+// merge of the terms' sorted rows: count (rowlen) or write (col, val) the
+// entries whose sum is not exactly 0.0
 template <bool FILL>
 __global__ void k_sum(SumArgs A, int32_t* rowlen, const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
                       double* __restrict__ val) {
@@ -128,6 +130,7 @@ __global__ void k_sum(SumArgs A, int32_t* rowlen, const int64_t* __restrict__ ro
             }
             v = __dadd_rn(v, x);
         }
+        if (v == 0.0) continue;  // map(+) drops sums that are exactly 0.0
         if (FILL) {
             col[w] = c;
             val[w] = v;

@@ -15,6 +15,8 @@ CASES = [(1, 3, 5, "sparse"), (2, 3, 4, "sparse"), (3, 2, 3, "sparse"), (2, 2, 3
 def same_bits(A, B):
     A = A.tocsr()
     B = B.tocsr()
+    A.sort_indices()
+    B.sort_indices()
     return (A.shape == B.shape and np.array_equal(A.indptr, B.indptr) and np.array_equal(A.indices, B.indices)
             and np.array_equal(A.data.view(np.int64), B.data.view(np.int64)))
 
@@ -25,6 +27,18 @@ def test_device_operators_equal_host(sgdg, D, k, n, scheme):
     op = sgdg.SparseGridOperator(D, k, n, scheme)
     for which in list(range(1, D + 1)) + [0, -1]:
         assert same_bits(op.device_csr(which), op.csr(which)), which
+    op.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,k,n,scheme", [(2, 3, 5, "sparse"), (3, 3, 4, "sparse"), (2, 2, 5, "sparse"),
+                                          (3, 2, 2, "full")])
+def test_device_laplacian_and_wave_rhs_equal_oracle(sgdg, O, D, k, n, scheme):
+    # the device merge drops the sums that cancel to exactly 0.0, as
+    # SparseArrays' map(+) does in laplacian_matrix (src/multidim_derivative.jl:71-79)
+    op = sgdg.SparseGridOperator(D, k, n, scheme)
+    assert same_bits(op.device_csr(0), O.laplacian_matrix(D, k, n, scheme))
+    assert same_bits(op.device_csr(-1), O.wave_rhs_raw(D, k, n, scheme).csc())
     op.close()
 
 
