@@ -15,7 +15,8 @@ value:  DOF-updates/s = state coefficients x RK stages / time, FP32
 e2e:    the same metric through the C ABI with host buffers: every timed step
         uploads all states from page-locked host memory, advances one RK4
         step and downloads all states.
-plain_fp64: the drop-in form (assembled FP64 CSR SpMV + FP64 RK4) on one solve.
+plain_fp64_batch: the drop-in form (assembled FP64 CSR SpMV + FP64 RK4) on the
+        same batch of solves, device-resident, at equal work.
 uneven_batch: 256 advection solves of uneven (D, k, n) in the same launches,
         with default and with autotuned tile shapes.
 vlasov: Vlasov transport in 2x2v phase space (k=2, n=8), FP64 sparse form.
@@ -56,7 +57,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--solves", type=int, default=256)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=50, help="calls per repeat of the end-to-end leg (3 repeats)")
     p.add_argument("--e2e-chunks", type=int, default=16, help="pipeline chunks of the end-to-end leg")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--vlasov-steps", type=int, default=500, help="RK4 steps of the 2x2v Vlasov leg (0: skip)")
@@ -90,21 +91,31 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def initial_states(sg, nsolves, seed0):
-    """Seeded 6-mode Fourier f0 and v0 per solve, wave vectors in [1,3]^3,
+def wave_modes(seed):
+    """Seeded 6-mode Fourier f0 and v0 of one solve, wave vectors in [1,3]^3,
     amplitudes U(-1,1) (the shape of the reference's traveling-wave inputs)."""
-    out = []
-    for s in range(nsolves):
-        rng = np.random.default_rng(seed0 + s)
-        fields = []
-        for _ in range(2):
-            modes = []
-            for _ in range(6):
-                a = tuple(int(v) for v in rng.integers(1, 4, size=D))
-                modes.append((a, float(rng.uniform(-1, 1)), "sin" if rng.random() < 0.5 else "cos", 0.0))
-            fields.append(sg.fourier_coeffs(D, K, NLEV, modes))
-        out.append(np.concatenate(fields))
-    return out
+    rng = np.random.default_rng(seed)
+    fields = []
+    for _ in range(2):
+        modes = []
+        for _ in range(6):
+            a = tuple(int(v) for v in rng.integers(1, 4, size=D))
+            modes.append((a, float(rng.uniform(-1, 1)), "sin" if rng.random() < 0.5 else "cos", 0.0))
+        fields.append(modes)
+    return fields
+
+
+def initial_states(fourier_coeffs, nsolves, seed0):
+    """[f0; v0] per solve from the seeded modes; fourier_coeffs is the
+    package's (the timed arms) or the oracle's (the reference arm)."""
+    return [np.concatenate([fourier_coeffs(D, K, NLEV, m) for m in wave_modes(seed0 + s)]) for s in range(nsolves)]
+
+
+def workload_config(solves, state_dofs):
+    """The workload both arms time: the same dict in both JSON lines."""
+    return {"workload": "wave3d_sparse_k3_n7_batch", "D": D, "k": K, "n": NLEV, "dt": DT,
+            "solves_per_gpu": solves, "state_dofs_per_solve": int(state_dofs),
+            "l2": "working set > 126 MB L2, no flush"}
 
 
 class Clocks:
@@ -300,9 +311,6 @@ def vlasov_leg(sg, stream, steps, batch=16):
     return out
 
 
-PLAIN_MEASURE_MAX_N = 1_100_000  # larger plain operators take minutes to assemble on the host
-
-
 def evaluate_leg(sg, stream, npts):
     """Point evaluation (reconstruct_DG) of a 3D sparse k=3, n=7 expansion
     (seeded Fourier coefficients) at npts uniform points, FP64 on the GPU:
@@ -376,13 +384,35 @@ def assembly_leg(sg, D=4, k=3, n=7):
             "nnz": int(z.value), "gpu_s": gpu_s, "host_s": host_s, "same_nnz": int(z.value) == int(nnz_host)}
 
 
+def plain_fifo(sg, reqs, y0s, ops):
+    """The plain per-request FP64 path run on the GPU as a single first-in-
+    first-out server in real time: each request, once it has arrived and the
+    previous one is done, assembles -sum_d a_d D_d on the GPU and runs its RK4
+    steps (advect_evolve, method plain, host state in and out).  Returns the
+    latencies, the results and the wall time from the first arrival to the
+    last completion."""
+    t0 = time.perf_counter() + 0.05
+    lat, results, last = [], [], t0
+    for r, y0 in zip(reqs, y0s):
+        arrive = t0 + r.t_arrival
+        wait = arrive - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        op = ops[(r.D, r.k, r.n)]
+        _, st = sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, r.nsteps * r.dt, nsteps=r.nsteps, method="plain", op=op)
+        last = time.perf_counter()
+        lat.append(last - arrive)
+        results.append(st[-1])
+    return np.array(lat), results, last - (t0 + reqs[0].t_arrival)
+
+
 def serving_leg(sg, args):
     """Poisson stream of advection requests of uneven (D, k, n) through the
     request loop (continuous batching), and the same stream through the plain
-    per-request FP64 path: a single first-in-first-out server whose service
-    time per request is measured on the GPU (assembly of sum_d a_d D_d and the
-    RK4 steps; the D_d of each (D, k, n) are cached, as a serving process
-    would) and replayed against the same arrival times."""
+    per-request FP64 path, run for real on the GPU as a FIFO server (the
+    index and 1D tables of each (D, k, n) built beforehand, as a serving
+    process would keep them); every served result is compared with its plain
+    FP64 result."""
     import importlib
     sv = importlib.import_module(sg.__name__ + ".serving")
     reqs = sv.poisson_stream(sg, args.serve_requests, args.serve_rate, seed=5)
@@ -402,45 +432,19 @@ def serving_leg(sg, args):
     ok = sum(1 for t in times if t[3] == srv.DONE)
     srv.close()
 
-    # plain per-request FP64 path: service time per (D, k, n) = fixed + steps x per-step
-    svc_model = {}
+    # plain per-request FP64 path, warmed with one step of every (D, k, n)
+    ops = {}
     for r, y0 in zip(reqs, y0s):
         key = (r.D, r.k, r.n)
-        if key in svc_model or y0.size > PLAIN_MEASURE_MAX_N:
-            continue
-        op = sg.SparseGridOperator(r.D, r.k, r.n)
-        sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, r.dt, nsteps=1, method="plain", op=op)  # builds D_d
-        t = []
-        for ns in (2, 12):
-            t0 = time.perf_counter()
-            sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, ns * r.dt, nsteps=ns, method="plain", op=op)
-            t.append(time.perf_counter() - t0)
-        per = max((t[1] - t[0]) / 10.0, 1e-9)
-        svc_model[key] = (max(t[0] - 2 * per, 0.0), per, y0.size)
+        if key not in ops:
+            ops[key] = sg.SparseGridOperator(r.D, r.k, r.n)
+            sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, r.dt, nsteps=1, method="plain", op=ops[key])
+    plain_lat, plain_res, plain_makespan = plain_fifo(sg, reqs, y0s, ops)
+    for op in ops.values():
         op.close()
-    # requests too large to assemble here: the measured per-DOF-update rate of the largest measured size
-    big_key = max(svc_model, key=lambda kk: svc_model[kk][2])
-    fixed_b, per_b, n_b = svc_model[big_key]
-    service, extrapolated = [], 0
-    for r, y0 in zip(reqs, y0s):
-        key = (r.D, r.k, r.n)
-        if key in svc_model:
-            fixed, per, _ = svc_model[key]
-        else:
-            fixed, per = fixed_b * y0.size / n_b, per_b * y0.size / n_b
-            extrapolated += 1
-        service.append(fixed + per * r.nsteps)
-    arr = np.array([r.t_arrival for r in reqs])
-    plain_lat = sv.fifo_latencies(arr, service)
-    plain_makespan = float(np.max(arr + plain_lat) - arr[0])
     total_dof = float(sum(4.0 * y.size * r.nsteps for r, y in zip(reqs, y0s)))
-
-    # accuracy of served results against the plain FP64 path (the smallest requests)
-    errs = []
-    for i in np.argsort([y.size * r.nsteps for r, y in zip(reqs, y0s)])[:4]:
-        r, y0 = reqs[i], y0s[i]
-        _, st = sg.advect_evolve(r.D, r.k, r.n, r.a, y0, 0.0, r.nsteps * r.dt, nsteps=r.nsteps, method="plain")
-        errs.append(float(np.linalg.norm(results[i] - st[-1]) / np.linalg.norm(st[-1])))
+    errs = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(results, plain_res)]
+    big = int(np.argmax([y.size for y in y0s]))
 
     return {
         "workload": "Poisson stream of advection solves, D 2-5, k 2-3, n 4-8, 100-1000 RK4 steps",
@@ -452,40 +456,47 @@ def serving_leg(sg, args):
         "plain_fp64_per_request": {"p50_latency_s": float(np.percentile(plain_lat, 50)),
                                    "p99_latency_s": float(np.percentile(plain_lat, 99)),
                                    "dof_updates_per_s": total_dof / plain_makespan, "makespan_s": plain_makespan,
-                                   "service_times": "measured per (D,k,n) on the GPU, FIFO replay of the arrivals",
-                                   "extrapolated_requests": extrapolated},
-        "rel_l2_vs_plain_fp64": {"max": max(errs), "requests": len(errs)},
+                                   "run": "FIFO on the GPU in real time, assembly of -sum_d a_d D_d per request"},
+        "rel_l2_vs_plain_fp64": {"max": max(errs), "median": float(np.median(errs)), "requests": len(errs),
+                                 "largest_request": {"D": reqs[big].D, "k": reqs[big].k, "n": reqs[big].n,
+                                                     "dofs": int(y0s[big].size), "steps": reqs[big].nsteps,
+                                                     "rel_l2": errs[big]}},
     }
 
 
+REF_SAMPLE_SOLVES = 16  # solves the reference arm advances per timed step
+
+
 def run_reference(args):
+    """The reference's CPU path on the host cores: Julia is not installed, so
+    the oracle's C restatement (FP64 CSR SpMV + RK4, OpenMP on every host
+    thread) advances a bounded sample of the batch's solves per step.  Only
+    the oracle is loaded (initial states from its own Fourier projection)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle import oracle as O
-    import __graft_entry__ as g
-    sg = g.load_package()
-    y0 = initial_states(sg, 1, 1000)[0]
     nth = O.max_threads()
+    sample = max(1, min(args.solves, REF_SAMPLE_SOLVES))
+    ys = initial_states(O.fourier_coeffs, sample, 1000)
     A = O.CSR(O.wave_rhs_raw(D, K, NLEV))
-    y = y0.copy()
     for _ in range(args.warmup):
-        y = A.rk4(y, DT, 1, nthreads=nth)
+        ys = [A.rk4(y, DT, 1, nthreads=nth) for y in ys]
     t = time.perf_counter()
     for _ in range(args.steps):
-        y = A.rk4(y, DT, 1, nthreads=nth)
+        ys = [A.rk4(y, DT, 1, nthreads=nth) for y in ys]
     el = time.perf_counter() - t
-    value = y0.size * 4.0 * args.steps / el
-    sample = "1 of the %d solves per step (solves are identical in cost), RK4 steps on the host" % args.solves
+    value = sample * ys[0].size * 4.0 * args.steps / el
+    desc = ("%d of the %d solves per step (every solve has the same operator and cost), one RK4 step each, "
+            "FP64 CSR oracle" % (sample, args.solves))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps * args.solves / sample,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Fourier ICs)",
-            "config": {"workload": "wave3d_sparse_k3_n7", "D": D, "k": K, "n": NLEV, "dt": DT,
-                       "state_dofs_per_solve": int(y0.size), "form": "FP64 CSR SpMV + FP64 RK4 (oracle port)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port", "sample": sample},
+            "data": "synthetic (seeded Fourier ICs)", "config": workload_config(args.solves, ys[0].size),
+            "form": "FP64 CSR SpMV + FP64 RK4 (the oracle's C restatement of the reference, OpenMP)",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "reference is Julia (not installed); its C restatement in oracle/ is timed"}
+            "note": "reference is Julia (not installed here or on the GPU host); its C restatement in oracle/ is timed"}
     print(json.dumps(line), flush=True)
 
 
@@ -506,7 +517,7 @@ def run_ours(args):
     # CUDA events below are recorded on it
     stream = torch.cuda.Stream(device=dev)
 
-    states = initial_states(sg, args.solves, 1000 + 100000 * rank)
+    states = initial_states(sg.fourier_coeffs, args.solves, 1000 + 100000 * rank)
     b = sg.Batch()
     ids = [b.add("wave", D, K, NLEV, y0, DT) for y0 in states]
     b.set_stream(stream.cuda_stream)
@@ -546,12 +557,16 @@ def run_ours(args):
     if dist:
         dist.barrier()
     # one call per step: host states in, one RK4 step, host states out, with
-    # the copies of each pipeline chunk overlapping the other chunks' steps
+    # the copies of each pipeline chunk overlapping the other chunks' steps;
+    # three repeats of e2e_steps calls, the median reported
     b.step_host(host.data_ptr(), host.data_ptr(), 1, args.e2e_chunks)  # builds the chunk graphs
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        b.step_host(host.data_ptr(), host.data_ptr(), 1, args.e2e_chunks)
-    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    reps = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            b.step_host(host.data_ptr(), host.data_ptr(), 1, args.e2e_chunks)
+        reps.append(max_over_ranks(time.perf_counter() - t0, dist, dev))
+    e2e_s = statistics.median(reps)
     e2e_value = job_rate(dofs_per_step, args.e2e_steps, world, e2e_s)
     # the same without the pipeline: upload, step, download in turn
     t0 = time.perf_counter()
@@ -560,17 +575,29 @@ def run_ours(args):
         b.step(1)
         b.download(host.data_ptr())
     e2e_serial = job_rate(dofs_per_step, args.e2e_steps, world, max_over_ranks(time.perf_counter() - t0, dist, dev))
+    b.close()
+    del host
 
-    # plain FP64 drop-in form on one solve (same problem)
+    # the plain FP64 drop-in form on the same batch: every solve's
+    # *(RHS, x) (src/pdes.jl:63) as an FP64 CSR SpMV fused with the RK4 stage
+    # update, all solves of a stage in one launch, states resident in HBM
     op = sg.SparseGridOperator(D, K, NLEV)
-    f0, v0 = states[0][:op.N], states[0][op.N:]
-    sg.wave_evolve(D, K, NLEV, f0, v0, 0.0, DT, nsteps=1, method="plain", op=op)  # assemble + upload once
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sg.wave_evolve(D, K, NLEV, f0, v0, 0.0, args.steps * DT, nsteps=args.steps, method="plain", op=op)
-    plain_s = time.perf_counter() - t0
-    plain_value = 2 * op.N * 4.0 * args.steps / plain_s
     plain_nnz = op.nnz(-1)
+    ydev = torch.tensor(np.concatenate(states), dtype=torch.float64, device=dev)
+    plain_warm, plain_steps = 3, max(3, min(args.steps, 20))
+    op.plain_steps_device(ydev.data_ptr(), args.solves, DT, plain_warm, stream=stream.cuda_stream)  # device operator
+    timings = []
+    for ns in (1, 1 + plain_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.plain_steps_device(ydev.data_ptr(), args.solves, DT, ns, stream=stream.cuda_stream)
+        timings.append(time.perf_counter() - t0)
+    plain_s = max_over_ranks(max(timings[1] - timings[0], 1e-9), dist, dev)  # the fixed cost of a call cancels
+    plain_value = job_rate(dofs_per_step, plain_steps, world, plain_s)
+    plain_done = plain_warm + 2 + plain_steps
+    plain_state0 = ydev[:states[0].size].cpu().numpy() if rank == 0 else None
+    del ydev
+    op.close()
 
     if rank != 0:
         if dist:
@@ -578,9 +605,12 @@ def run_ours(args):
         return
 
     cpu = None
+    from oracle import oracle as O
     if not args.no_cpu:
-        from oracle import oracle as O
         cpu = cpu_oracle_leg(states[0], gpu_state0, args.warmup + args.steps, O.max_threads())
+    # the plain batch's solve 0 against the oracle after the same steps
+    ref0 = O.CSR(O.wave_rhs_raw(D, K, NLEV)).rk4(states[0], DT, plain_done, nthreads=O.max_threads())
+    plain_err = float(np.linalg.norm(plain_state0 - ref0) / np.linalg.norm(ref0))
 
     peak, peak_kind = measured_peak_hbm()
     step_s = ms / 1e3 / args.steps
@@ -595,10 +625,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 apply / f64 RK state", "data": "synthetic (seeded Fourier ICs)",
-        "config": {"workload": "wave3d_sparse_k3_n7_batch", "D": D, "k": K, "n": NLEV, "dt": DT,
-                   "solves_per_gpu": args.solves, "state_dofs_per_solve": int(total // args.solves),
-                   "working_set_bytes_per_gpu": int(working_set), "l2": "working set > 126 MB L2, no flush",
-                   "form": "matrix-free FP32 pencil apply, FP64 RK4, CUDA graph per step"},
+        "config": workload_config(args.solves, total // args.solves),
+        "form": "matrix-free FP32 pencil apply, FP64 RK4, CUDA graph per step",
+        "working_set_bytes_per_gpu": int(working_set), "tile_shape_wlog_coop": list(tile[:2]),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(total * 8),
                 "d2h_bytes_per_step": int(total * 8), "steps": args.e2e_steps, "pipeline_chunks": args.e2e_chunks,
                 "serial_upload_step_download": e2e_serial},
@@ -606,11 +635,14 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,
                      "bytes_per_dof_update": BYTES_PER_DOF_UPDATE},
-        "plain_fp64": {"value": plain_value, "unit": UNIT, "solves": 1, "nnz": int(plain_nnz),
-                       "ms_per_step": 1e3 * plain_s / args.steps},
+        "plain_fp64_batch": {"form": "FP64 CSR SpMV + FP64 RK4 stage update per solve, all solves of a stage in "
+                                     "one launch, CUDA graph per step (sgdg_op_plain_steps_device)",
+                             "value": plain_value, "unit": UNIT, "solves": args.solves, "nnz": int(plain_nnz),
+                             "steps": plain_steps, "ms_per_step": 1e3 * plain_s / plain_steps,
+                             "chosen_over_plain": value / plain_value,
+                             "rel_l2_vs_oracle": {"value": plain_err, "solve": 0, "steps": plain_done}},
         "clocks": clocks,
     }
-    line["config"]["tile_shape_wlog_coop"] = list(tile[:2])
     line["uneven_batch"] = uneven_batch_leg(sg, stream)
     if args.vlasov_steps > 0:
         line["vlasov"] = vlasov_leg(sg, stream, args.vlasov_steps)

@@ -326,6 +326,13 @@ class SparseGridOperator:
         check(lib().sgdg_apply_device(self._h, which, _method(method), ctypes.c_void_p(x_ptr),
                                       ctypes.c_void_p(y_ptr), ctypes.c_void_p(stream)))
 
+    def plain_steps_device(self, y_ptr, nsolves, dt, nsteps, which=-1, stream=0):
+        """nsteps plain FP64 RK4 steps of y' = A y (A = operator `which`, the
+        wave right-hand side by default) for nsolves device-resident states
+        stored one after another at y_ptr, updated in place."""
+        check(lib().sgdg_op_plain_steps_device(self._h, int(which), int(nsolves), ctypes.c_void_p(y_ptr), float(dt),
+                                               int(nsteps), ctypes.c_void_p(stream)))
+
 
 def D_matrix(D, d, k, n, scheme="sparse"):
     """D-dimensional derivative along dim d, 1-based (src/multidim_derivative.jl:61-65)."""

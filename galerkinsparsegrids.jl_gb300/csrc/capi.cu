@@ -20,6 +20,8 @@
 namespace sgdg {
 
 cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st);
+cudaError_t launch_csr_rk4_batch(const DevCSR& A, int64_t nb, int64_t bs, const double* uin, double* y, double* acc,
+                                 double* uout, double dt, int stage, cudaStream_t st);
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
                            int stage, cudaStream_t st);
 cudaError_t launch_csr_spmv_multi(const DevCSR& A, int nv, const double* x, int64_t xi, int64_t xs, double* y,
@@ -493,6 +495,52 @@ static void plain_evolve(sgdg_op* op, int which_or_adv, const DeviceCSR* Aadv, c
     if (err != cudaSuccess) throw Error(SGDG_ECUDA, std::string("evolve: ") + cudaGetErrorString(err));
 }
 
+// nsteps plain FP64 RK4 steps of nsolves solves y' = A y sharing operator
+// `which`, states device-resident one after another; one RK4 step (four
+// batched stage launches) is captured as a graph and replayed.
+static void plain_batch_steps(sgdg_op* op, int which, int64_t nsolves, double* y, double dt, int64_t nsteps,
+                              cudaStream_t st) {
+    const DevCSR& A = op->device(which);
+    const int64_t len = A.m, total = nsolves * len;
+    DevBuf acc(sizeof(double) * total), u0(sizeof(double) * total), u1(sizeof(double) * total);
+    cudaStream_t cs = st;
+    cudaStream_t own = nullptr;
+    if (cs == nullptr) {  // graphs cannot be captured on the legacy stream
+        CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        cs = own;
+        CK(cudaStreamSynchronize(nullptr));
+    }
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    double* a = acc.as<double>();
+    double* p0 = u0.as<double>();
+    double* p1 = u1.as<double>();
+    cudaError_t e = launch_csr_rk4_batch(A, nsolves, len, y, y, a, p0, dt, 1, cs);
+    if (e == cudaSuccess) e = launch_csr_rk4_batch(A, nsolves, len, p0, y, a, p1, dt, 2, cs);
+    if (e == cudaSuccess) e = launch_csr_rk4_batch(A, nsolves, len, p1, y, a, p0, dt, 3, cs);
+    if (e == cudaSuccess) e = launch_csr_rk4_batch(A, nsolves, len, p0, y, a, p1, dt, 4, cs);
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (own) cudaStreamDestroy(own);
+        throw Error(SGDG_ECUDA, std::string("capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) {
+        if (own) cudaStreamDestroy(own);
+        throw Error(SGDG_ECUDA, std::string("instantiate: ") + cudaGetErrorString(e3));
+    }
+    cudaError_t err = cudaSuccess;
+    for (int64_t i = 0; i < nsteps && err == cudaSuccess; i++) err = cudaGraphLaunch(ge, cs);
+    // the scratch vectors are freed on return: wait for the steps
+    if (err == cudaSuccess) err = cudaStreamSynchronize(cs);
+    cudaGraphExecDestroy(ge);
+    if (own) cudaStreamDestroy(own);
+    if (err != cudaSuccess) throw Error(SGDG_ECUDA, std::string("plain batch: ") + cudaGetErrorString(err));
+}
+
 static void mf_evolve(sgdg_op* op, int kind, const double* a, const double* y0, int64_t len, double t0, double t1,
                       int64_t nsteps, int nout, double* times, double* states) {
     cudaStream_t st = op_stream(op);
@@ -521,6 +569,19 @@ static void check_evolve_args(int64_t nsteps, int nout, double t0, double t1) {
     if (nsteps < 1) throw Error(SGDG_EINVAL, "nsteps must be >= 1");
     if (nout < 2) throw Error(SGDG_EINVAL, "nout must be >= 2");
     if (!(std::isfinite(t0) && std::isfinite(t1)) || t1 == t0) throw Error(SGDG_EINVAL, "need finite t0 != t1");
+}
+
+int sgdg_op_plain_steps_device(sgdg_op* op, int which, int64_t nsolves, double* y_dev, double dt, int64_t nsteps,
+                               void* stream) {
+    API_BEGIN
+    NEED(op);
+    NEED(y_dev);
+    if (nsolves < 1) throw Error(SGDG_EINVAL, "nsolves must be >= 1");
+    if (nsteps < 0) throw Error(SGDG_EINVAL, "nsteps must be >= 0");
+    if (!std::isfinite(dt)) throw Error(SGDG_EINVAL, "dt must be finite");
+    require_gpu();
+    if (nsteps > 0) plain_batch_steps(op, which, nsolves, y_dev, dt, nsteps, (cudaStream_t)stream);
+    API_END
 }
 
 int sgdg_wave_evolve(sgdg_op* op, const double* f0, const double* v0, double t0, double t1, int64_t nsteps, int nout,

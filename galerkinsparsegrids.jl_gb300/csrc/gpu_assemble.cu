@@ -440,10 +440,11 @@ __global__ void __launch_bounds__(32 * kTRowsPerBlock)
     int64_t ntup = 1;
     for (int d = 0; d < D; d++) ntup *= ng[d];
     // an empty 1D row: no entries in row i; a long row: k_transform_long,
-    // launched after this kernel, overwrites the 0 (every row's count is
-    // written here, so no row pointer comes from an unwritten count)
+    // launched after this kernel for the rows the host listed, overwrites the
+    // -1 (every row's count is written here, and a long row the host did not
+    // list keeps -1, which the row-pointer scan rejects)
     if (ntup == 0 || ntup >= kTLongTuples) {
-        if (!FILL && lane == 0) rowlen[i] = 0;
+        if (!FILL && lane == 0) rowlen[i] = ntup == 0 ? 0 : -1;
         return;  // the whole warp
     }
     int64_t w = FILL ? rowptr[i] : 0;

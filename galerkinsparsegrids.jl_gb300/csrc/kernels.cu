@@ -196,9 +196,18 @@ __device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, const double* 
     }
 }
 
+// blockIdx.y selects one of several solves sharing A (RK only): its vectors
+// sit bs elements after the previous solve's
 template <int NV, int W, bool RK>
 __global__ void __launch_bounds__(256) k_csr(DevCSR A, const double* __restrict__ x, int64_t xi, int64_t xs,
-                                             double* y, int64_t yi, int64_t ys, CsrRK rk) {
+                                             double* y, int64_t yi, int64_t ys, CsrRK rk, int64_t bs) {
+    if constexpr (RK) {
+        const int64_t o = (int64_t)blockIdx.y * bs;
+        x += o;
+        y += o;
+        rk.acc += o;
+        rk.uout += o;
+    }
     int bin = 0;
     while (bin + 1 < kCsrBins && (int)blockIdx.x >= A.bin_block[bin + 1]) bin++;
     switch (bin) {
@@ -316,7 +325,8 @@ static int grid_for(int64_t threads) {
 template <int NV, int W, bool RK>
 static void csr_pass(const DevCSR& A, const double* x, int64_t xi, int64_t xs, double* y, int64_t yi, int64_t ys,
                      const CsrRK& rk, cudaStream_t st) {
-    if (A.bin_block[kCsrBins] > 0) k_csr<NV, W, RK><<<A.bin_block[kCsrBins], 256, 0, st>>>(A, x, xi, xs, y, yi, ys, rk);
+    if (A.bin_block[kCsrBins] > 0)
+        k_csr<NV, W, RK><<<A.bin_block[kCsrBins], 256, 0, st>>>(A, x, xi, xs, y, yi, ys, rk, 0);
     if (A.nlong > 0) {
         k_csr_segments<NV, W><<<grid_for(A.nseg * 32), 256, 0, st>>>(A, x, xi, xs);
         k_csr_long_rows<<<grid_for(A.nlong * NV), 256, 0, st>>>(A, NV, y, yi, ys, rk, RK);
@@ -362,6 +372,24 @@ cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double
                            int stage, cudaStream_t st) {
     const CsrRK rk{acc, uout, dt, 0.5 * dt, dt / 6.0, stage};
     csr_pass<1, 1, true>(A, uin, 1, 0, y, 1, 0, rk, st);
+    return cudaGetLastError();
+}
+
+// One RK4 stage of nb solves that share A, their vectors one after another
+// (solve s at s * bs): the row kernel with one grid row per solve; a matrix
+// with long rows (segment partials) takes one pass per solve.
+cudaError_t launch_csr_rk4_batch(const DevCSR& A, int64_t nb, int64_t bs, const double* uin, double* y, double* acc,
+                                 double* uout, double dt, int stage, cudaStream_t st) {
+    const CsrRK rk{acc, uout, dt, 0.5 * dt, dt / 6.0, stage};
+    if (A.nlong == 0 && nb <= 65535) {
+        if (A.bin_block[kCsrBins] > 0 && nb > 0)
+            k_csr<1, 1, true><<<dim3(A.bin_block[kCsrBins], (unsigned)nb), 256, 0, st>>>(A, uin, 1, 0, y, 1, 0, rk, bs);
+        return cudaGetLastError();
+    }
+    for (int64_t s = 0; s < nb; s++) {
+        const CsrRK r{acc + s * bs, uout + s * bs, dt, 0.5 * dt, dt / 6.0, stage};
+        csr_pass<1, 1, true>(A, uin + s * bs, 1, 0, y + s * bs, 1, 0, r, st);
+    }
     return cudaGetLastError();
 }
 

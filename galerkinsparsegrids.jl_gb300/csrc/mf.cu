@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <map>
+#include <mutex>
 
 #include "engine.h"
 #include "cvt.cuh"
@@ -545,9 +547,25 @@ cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* clas
     return cudaGetLastError();
 }
 
+// The dynamic shared-memory limit of k_mf_stage is one attribute per device
+// for the whole process, and every engine (and the allocation-free entry
+// point) launches with the size it planned: so the limit only ever rises,
+// to the largest size any caller has asked for on that device.
 cudaError_t mf_configure(size_t smem, int* blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(k_mf_stage, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::mutex mu;
+    static std::map<int, size_t> limit;  // device -> attribute value set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        size_t& cur = limit[dev];
+        if (smem > cur) {
+            e = cudaFuncSetAttribute(k_mf_stage, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            cur = smem;
+        }
+    }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_mf_stage, kMFThreads, smem);
 }
 

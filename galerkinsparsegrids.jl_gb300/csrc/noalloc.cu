@@ -104,6 +104,13 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         const SparseIndex ix = make_index(D, k, n, scheme);
         if (!(which == SGDG_OP_LAPLACIAN || (which >= 1 && which <= D)))
             return noalloc_fail(SGDG_EINVAL, "which must be 1..D (D_d) or 0 (laplacian)");
+        // the FP32 copy of x and the FP32 partial sums alone must fit: reject
+        // before the pencils and the work list are built on the host
+        if (ix.N > (int64_t)INT32_MAX || 2 * sizeof(float) * (size_t)ix.N > kNoAllocScratchBytes)
+            return noalloc_fail(SGDG_EINVAL, "problem of " + std::to_string(ix.N) +
+                                                 " coefficients needs more scratch than sgdg_apply_noalloc holds: "
+                                                 "at most " + std::to_string(kNoAllocScratchBytes) +
+                                                 " bytes (use sgdg_apply_device for larger problems)");
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
             cudaGetLastError();

@@ -121,6 +121,16 @@ int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, const double 
  * state), like ODE.jl's (times, states) at the requested output points. */
 int sgdg_wave_evolve(sgdg_op *op, const double *f0, const double *v0, double t0, double t1, int64_t nsteps,
                      int nout, int method, double *times, double *states);
+/* The plain form's stepping for many solves that share one operator: nsteps
+ * classical RK4 steps of y' = A y, A the assembled FP64 operator `which`
+ * (SGDG_OP_WAVE_RHS for wave_evolve's [[0, I], [L, 0]], SGDG_OP_LAPLACIAN or
+ * 1..D), for nsolves states held on the device one after another (y_dev:
+ * nsolves * size of A doubles, updated in place), dt fixed.  Each stage is
+ * the FP64 CSR SpMV *(RHS, x) of src/pdes.jl:63 fused with the RK4 stage
+ * update, launched over all solves at once; returns once the steps are done
+ * on `stream` (cudaStream_t, may be NULL). */
+int sgdg_op_plain_steps_device(sgdg_op *op, int which, int64_t nsolves, double *y_dev, double dt, int64_t nsteps,
+                               void *stream);
 /* Linear advection f_t = -sum_d a_d D_d f (velocity a[D]), composed from
  * grad_matrix the way wave_evolve composes laplacian_matrix. */
 int sgdg_advect_evolve(sgdg_op *op, const double *a, const double *f0, double t0, double t1, int64_t nsteps,

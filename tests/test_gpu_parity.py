@@ -183,3 +183,28 @@ def test_batch_remove_and_budget(sgdg):
         assert e.value.code == 2
     finally:
         sgdg.set_hbm_budget(0)
+
+
+def test_plain_steps_for_many_solves(sgdg, O):
+    # sgdg_op_plain_steps_device: the plain form for several solves sharing
+    # the wave right-hand side (src/pdes.jl:63 per solve), device-resident;
+    # each solve equals its own plain wave_evolve bit for bit and the oracle
+    # to 1e-10
+    torch = pytest.importorskip("torch")
+    D, k, n, steps = 2, 3, 4, 25
+    t1 = steps * 2e-3
+    dt = (t1 - 0.0) / steps  # the step wave_evolve derives from (t0, t1, nsteps)
+    op = sgdg.SparseGridOperator(D, k, n)
+    ys = [np.concatenate([fourier_ic(sgdg, D, k, n, 3, seed=40 + s), fourier_ic(sgdg, D, k, n, 2, seed=50 + s)])
+          for s in range(3)]
+    dev = torch.tensor(np.concatenate(ys), dtype=torch.float64, device="cuda")
+    op.plain_steps_device(dev.data_ptr(), len(ys), dt, steps)
+    got = dev.cpu().numpy().reshape(len(ys), -1)
+    A = O.CSR(O.wave_rhs_raw(D, k, n))
+    for s, y0 in enumerate(ys):
+        _, st = sgdg.wave_evolve(D, k, n, y0[:op.N], y0[op.N:], 0.0, t1, nsteps=steps, method="plain", op=op)
+        assert np.array_equal(got[s], st[-1]), s
+        assert rel(got[s], A.rk4(y0, dt, steps)) < 1e-10, s
+    with pytest.raises(sgdg.SGDGError):
+        op.plain_steps_device(dev.data_ptr(), 0, dt, 1)
+    op.close()

@@ -69,6 +69,49 @@ def test_noalloc_matches_existing_entry_point_twice(sgdg):
     assert torch.cuda.mem_get_info()[0] == before
 
 
+# Shapes that take every path of the entry point: k <= 3 (four columns per
+# thread) and k = 4, 5 (two), D = 1 (one phase, no wait), the 1D table in
+# shared memory and (k = 3, n = 10: ~82 KB) in global memory.
+SHAPES = [(1, 2, 6), (2, 5, 5), (4, 4, 4), (1, 3, 10), (3, 2, 4)]
+
+
+@pytest.mark.parametrize("D,k,n", SHAPES)
+def test_noalloc_shapes_match_existing_and_oracle(sgdg, O, D, k, n):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    op = sgdg.SparseGridOperator(D, k, n)
+    rng = np.random.default_rng(7 + D + 10 * k + 100 * n)
+    for which in list(range(1, D + 1)) + [0]:
+        xh = rng.standard_normal(op.N)
+        x = torch.tensor(xh, dtype=torch.float64, device="cuda")
+        ref = _existing(sgdg, torch, op, which, x)
+        got = _noalloc(sgdg, torch, D, k, n, which, x)
+        assert _rel(got, ref) <= TOL, (which, _rel(got, ref))
+        # and against the FP64 oracle's assembled operator
+        A = O.laplacian_matrix_raw(D, k, n) if which == 0 else O.D_matrix_raw(D, which, k, n)
+        assert _rel(got, O.spmv_csc(A, xh)) <= TOL, (which, "oracle")
+    op.close()
+
+
+def test_noalloc_leaves_planned_engines_launchable(sgdg):
+    # The kernel's dynamic shared-memory limit is process-wide: a no-alloc
+    # call on a small problem must not lower it below what an engine planned
+    # for a larger one, or that engine's next launch would be refused.
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    big = sgdg.SparseGridOperator(3, 3, 6)
+    rng = np.random.default_rng(3)
+    xb = torch.tensor(rng.standard_normal(big.N), dtype=torch.float64, device="cuda")
+    first = _existing(sgdg, torch, big, 1, xb)
+    xs = torch.tensor(rng.standard_normal(sgdg.get_size(2, 2, 3)), dtype=torch.float64, device="cuda")
+    _noalloc(sgdg, torch, 2, 2, 3, 1, xs)
+    again = _existing(sgdg, torch, big, 1, xb)
+    assert np.array_equal(first, again)
+    big.close()
+
+
 def test_noalloc_rejects_problems_beyond_its_scratch(sgdg):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
