@@ -8,7 +8,7 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM_BUDGET, ETIMEOUT, ECUDA, ECANCELLED, ENOGPU, EUNSUPPORTED, EIO = range(9)
+OK, EINVAL, ENOMEM_BUDGET, ETIMEOUT, ECUDA, ECANCELLED, ENOGPU, EUNSUPPORTED, EIO, ENONFINITE = range(10)
 SCHEMES = {"sparse": 0, "full": 1}
 METHODS = {"plain": 0, "matfree": 1}
 KIND_ADVECT, KIND_WAVE = 0, 1

@@ -100,6 +100,18 @@ class Server {
             Request& r = reqs_[id];
             eng_.remove(r.eid);
             r.eid = -1;
+            // a solve whose state is no longer finite (a NaN or infinity in its
+            // input, or a step beyond stability) fails alone: its columns
+            // never mix with other requests' arithmetic
+            int64_t bad = -1;
+            for (int64_t i = 0; i < r.Ns && bad < 0; i++)
+                if (!std::isfinite(r.result[i])) bad = i;
+            if (bad >= 0) {
+                fail(r, SGDG_ENONFINITE, "state not finite after " + std::to_string(r.steps_done) +
+                                             " steps (first at coefficient " + std::to_string(bad) + ")");
+                r.result.clear();
+                continue;
+            }
             r.state = SGDG_REQ_DONE;
             r.t_done = now();
         }

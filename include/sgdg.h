@@ -36,7 +36,8 @@ enum {
     SGDG_ECANCELLED = 5,      /* the request was cancelled                                     */
     SGDG_ENOGPU = 6,          /* no usable CUDA device                                         */
     SGDG_EUNSUPPORTED = 7,    /* valid input outside what this build implements                */
-    SGDG_EIO = 8              /* a file could not be opened or written                         */
+    SGDG_EIO = 8,             /* a file could not be opened or written                         */
+    SGDG_ENONFINITE = 9       /* a served solve's state is no longer finite (NaN or infinity)   */
 };
 
 enum { SGDG_SCHEME_SPARSE = 0, SGDG_SCHEME_FULL = 1 };
