@@ -444,6 +444,93 @@ MFOperator mf_operator(int k, int n) {
     return mf_table(k, n, op->nblocks, op->rowptr, op->colblk, op->val, 1e-10);
 }
 
+// The wave applies D_d D_d; on a pencil's line D_d is the leading block B of
+// the 1D operator for the line length lm, so D_d D_d is B B there (not the
+// leading block of the squared operator: the inner sum stops at the line's
+// finest level).  B B has the block pattern of B once blocks at roundoff are
+// dropped (a fine/coarse pair meets only at the coarse function's breaks,
+// as for B), so one sweep of B B costs half of two sweeps of B.  The table
+// holds B B of the pruned B for every lm = 1..n+1, in FP64 before the hi/lo
+// split; blocks below 1e-10 of the largest entry of their lm are dropped.
+MFSquareTables mf_square_tables(int k, int n) {
+    auto op = dlf1d(k, n);
+    double vmax = 0.0;
+    for (double v : op->val) vmax = std::max(vmax, std::fabs(v));
+    // the pruned blocks of the 1D operator, by row block
+    const int nb = op->nblocks, kk = k * k;
+    std::vector<std::vector<std::pair<int, const double*>>> rows(nb);
+    for (int rb = 0; rb < nb; rb++)
+        for (int p = op->rowptr[rb]; p < op->rowptr[rb + 1]; p++) {
+            const double* b = &op->val[(size_t)p * kk];
+            double bmax = 0.0;
+            for (int t = 0; t < kk; t++) bmax = std::max(bmax, std::fabs(b[t]));
+            if (bmax > 1e-10 * vmax) rows[rb].push_back({op->colblk[p], b});
+        }
+    MFSquareTables Q;
+    Q.k = k;
+    Q.n = n;
+    Q.rs = ((2 * k + 3) / 4) * 4;
+    std::map<std::vector<long long>, int> ids;
+    for (int lm = 1; lm <= n + 1; lm++) {
+        const int nrb = 1 << (lm - 1);
+        std::vector<std::map<int, std::vector<double>>> sq(nrb);
+        double smax = 0.0;
+        for (int rb = 0; rb < nrb; rb++) {
+            for (const auto& pb : rows[rb]) {
+                if (pb.first >= nrb) continue;
+                for (const auto& cb : rows[pb.first]) {
+                    if (cb.first >= nrb) continue;
+                    std::vector<double>& acc = sq[rb][cb.first];
+                    if (acc.empty()) acc.assign(kk, 0.0);
+                    for (int i = 0; i < k; i++)
+                        for (int j = 0; j < k; j++) {
+                            double t = 0.0;
+                            for (int q = 0; q < k; q++) t += pb.second[i * k + q] * cb.second[q * k + j];
+                            acc[i * k + j] += t;
+                        }
+                }
+            }
+            for (auto& e : sq[rb])
+                for (double v : e.second) smax = std::max(smax, std::fabs(v));
+        }
+        Q.roff.push_back((int32_t)Q.rowptr.size());
+        Q.rowptr.push_back((int32_t)Q.ent.size());
+        for (int rb = 0; rb < nrb; rb++) {
+            for (auto& e : sq[rb]) {
+                const std::vector<double>& b = e.second;
+                double bmax = 0.0;
+                for (double v : b) bmax = std::max(bmax, std::fabs(v));
+                if (bmax <= 1e-10 * smax) continue;
+                std::vector<long long> key(kk);
+                for (int t = 0; t < kk; t++) key[t] = std::llround(b[t] / smax * 1e12);
+                key.push_back(lm);  // values are compared within one line length's scale
+                auto it = ids.find(key);
+                int id;
+                if (it == ids.end()) {
+                    id = Q.ndist++;
+                    ids.emplace(std::move(key), id);
+                    const size_t base = Q.val.size();
+                    Q.val.resize(base + (size_t)k * Q.rs, 0.f);
+                    for (int i = 0; i < k; i++)
+                        for (int j = 0; j < k; j++) {
+                            const double x = b[i * k + j];
+                            const float hi = (float)x;
+                            Q.val[base + (size_t)i * Q.rs + 2 * j] = hi;
+                            Q.val[base + (size_t)i * Q.rs + 2 * j + 1] = (float)(x - (double)hi);
+                        }
+                } else {
+                    id = it->second;
+                }
+                if (id >= 4096 || e.first >= (1 << 19))
+                    throw Error(7, "squared line operators too large for the matrix-free block table");
+                Q.ent.push_back((e.first << 12) | id);
+            }
+            Q.rowptr.push_back((int32_t)Q.ent.size());
+        }
+    }
+    return Q;
+}
+
 MFOperator mf_transform_table(int k, int n, int which) {
     // element CSR of the 1D map -> dense k x k blocks per (level, cell) pair
     const CSR T = transform_1d(k, n, which);

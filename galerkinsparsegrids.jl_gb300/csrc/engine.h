@@ -55,12 +55,23 @@ enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1, MF_KIND_VLASOV = 2 };
 enum : int {
     TILE_FIRST = 1, TILE_LAST = 2, TILE_RK = 4, TILE_STORE = 8, TILE_WACC = 16, TILE_WAIT_IN = 32, TILE_SUMIN = 64
 };
-enum : int { TABLE_DERIVATIVE = -1 };  // MFItem::tab; 0..3: the nodal transforms
+// MFItem::tab; 0..3: the nodal transforms.  TABLE_SQUARE: the wave's
+// D_d D_d on the pencil's line as one sweep of the squared line operator
+// (otherwise the wave sweeps the derivative table twice).
+enum : int { TABLE_DERIVATIVE = -1, TABLE_SQUARE = -2 };
+constexpr int kMFMaxLevels = 16;  // n + 1 <= 16 line lengths per class
 
 struct MFClass {
     const int32_t* s_rowptr;  // 1D operator, block CSR over 2^n row blocks (2^n + 1 entries)
     const int32_t* s_ent;     // per stored block: column block << 12 | distinct block id
     const float* s_val;       // distinct blocks: k rows of (hi, lo) pairs, each row padded to rs floats
+    // the squared line operators (wave): one block-CSR table per line length
+    // lm = 1..n+1 (its 2^(lm-1) + 1 row pointers at q_rowptr + q_roff[lm - 1],
+    // indexing q_ent); the distinct blocks are shared by all line lengths
+    const int32_t* q_rowptr;
+    const int32_t* q_ent;
+    const float* q_val;
+    int32_t q_roff[kMFMaxLevels];
     const int64_t* blockoff;  // level-block offsets of every pencil of the class
     double* y;                // arenas, nslots * Ns
     double* acc;

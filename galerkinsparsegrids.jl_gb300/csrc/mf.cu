@@ -188,7 +188,7 @@ __device__ __forceinline__ void tile_columns(int W, int lw, ColFn&& col) {
 // level's cell count) are tabulated once per tile in shared memory.
 constexpr int kOutRows = 4;       // rows per batch of the output loops
 
-template <int K, int CPT, bool WAVE>
+template <int K, int CPT, bool WAVE, bool TWICE>
 __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int stage, int in_sel, float* smem,
                           int* ctr, int* err, int* claim) {
     const int tid = threadIdx.x;
@@ -283,15 +283,15 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
                 *reinterpret_cast<float2*>(yp) = make_float2(o[i][0], o[i][1]);
         }
     };
-    // result Z of the tile: wave X -> Y -> X (X is dead after the first
-    // sweep), advection X -> Y
+    // result Z of the tile: X -> Y, or for the wave's D_d D_d without the
+    // squared table X -> Y -> X (X is dead after the first sweep)
     float* Z = Y;
-    if (WAVE) {
+    if (TWICE) {
         apply_rows<K, CPT>(T, X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Y, rb, jq, o); });
         __syncthreads();
         Z = X;
     }
-    apply_rows<K, CPT>(T, WAVE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Z, rb, jq, o); });
+    apply_rows<K, CPT>(T, TWICE ? Y : X, W, nrb, lwq, rlong, [&](int rb, int jq, float(&o)[K][CPT]) { store(Z, rb, jq, o); });
     // the partial sums of this group's previous pass must be complete
     if (!(it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
     __syncthreads();
@@ -491,7 +491,9 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             done = it.done_ctr;
         }
         OpTable T{C.s_rowptr, C.s_ent, C.s_val};
-        if (it.tab != TABLE_DERIVATIVE) {  // a nodal transform: read through L1
+        if (it.tab == TABLE_SQUARE) {  // the wave's squared line operator: read through L1
+            T = OpTable{C.q_rowptr + C.q_roff[it.lmax - 1], C.q_ent, C.q_val};
+        } else if (it.tab != TABLE_DERIVATIVE) {  // a nodal transform: read through L1
             T = OpTable{C.t_rowptr[it.tab], C.t_ent[it.tab], C.t_val[it.tab]};
         } else if (C.s_shared) {
             int* trow = reinterpret_cast<int*>(smem);
@@ -507,17 +509,25 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             }
             T = OpTable{trow, tent, tval};
         }
-        switch (C.k * 2 + (C.kind == MF_KIND_WAVE ? 1 : 0)) {  // Vlasov sweeps once, like advection
-            case 2: pass_tile<1, 4, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 3: pass_tile<1, 4, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 4: pass_tile<2, 4, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 5: pass_tile<2, 4, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 6: pass_tile<3, 4, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 7: pass_tile<3, 4, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 8: pass_tile<4, 2, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 9: pass_tile<4, 2, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 10: pass_tile<5, 2, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 11: pass_tile<5, 2, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+        // Vlasov sweeps once, like advection; the wave twice unless its
+        // squared table is used
+        const int kind = C.kind != MF_KIND_WAVE ? 0 : it.tab == TABLE_SQUARE ? 1 : 2;
+        switch (C.k * 3 + kind) {
+            case 3: pass_tile<1, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 4: pass_tile<1, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 5: pass_tile<1, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 6: pass_tile<2, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 7: pass_tile<2, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 8: pass_tile<2, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 9: pass_tile<3, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 10: pass_tile<3, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 11: pass_tile<3, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 12: pass_tile<4, 2, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 13: pass_tile<4, 2, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 14: pass_tile<4, 2, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 15: pass_tile<5, 2, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 16: pass_tile<5, 2, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 17: pass_tile<5, 2, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
             default:
                 if (tid == 32) s_item = nitems;  // unreachable (k in 1..5): stop
                 break;

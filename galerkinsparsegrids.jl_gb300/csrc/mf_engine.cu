@@ -9,6 +9,7 @@
 // a CUDA graph; a membership change drops the graph and the next step
 // re-captures it.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -24,6 +25,21 @@ cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
 
 static constexpr size_t kWaveLag = 3;       // steps between a group's consecutive phases in the work list
+
+// The wave's D_d D_d on a pencil of line length lmax: one sweep of the
+// squared line operator for lmax <= kWaveSquareLevels, two sweeps of the
+// line operator above.  One sweep halves the FP32 work, but its partial
+// sums cancel more (entries grow like 4^l instead of 2^l), so the long
+// lines keep two sweeps: 3D k=3 n=7 to t=1 stays at 7.3e-7 relative L2
+// (7.4e-7 with two sweeps everywhere, 2.7e-6 with one sweep everywhere).
+constexpr int kWaveSquareLevels = 5;
+static int wave_square_levels() {  // SGDG_MF_WAVE_SQUARE overrides (0: two sweeps everywhere)
+    static const int lv = [] {
+        const char* e = std::getenv("SGDG_MF_WAVE_SQUARE");
+        return e ? std::max(0, std::atoi(e)) : kWaveSquareLevels;
+    }();
+    return lv;
+}
 constexpr int64_t kGroupReuseBytes = 6LL << 20;  // reused u + rhs per group (~4 groups in flight)
 
 // The arenas' cudaFree calls wait for outstanding work; the stream is not
@@ -174,6 +190,21 @@ const MFEngine::TTables& MFEngine::ttab(int k, int n) {
     }
     CK(cudaStreamSynchronize(stream_));
     return ttabs_.emplace(key, std::move(T)).first->second;
+}
+
+const MFEngine::QTable& MFEngine::qtab(int k, int n) {
+    auto key = std::make_pair(k, n);
+    auto it = qtabs_.find(key);
+    if (it != qtabs_.end()) return it->second;
+    const MFSquareTables Q = mf_square_tables(k, n);
+    if ((int)Q.roff.size() > kMFMaxLevels) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports n <= 15");
+    QTable T;
+    T.rowptr = upload(Q.rowptr, stream_);
+    T.ent = upload(Q.ent, stream_);
+    T.val = upload(Q.val, stream_);
+    T.roff = Q.roff;
+    CK(cudaStreamSynchronize(stream_));
+    return qtabs_.emplace(key, std::move(T)).first->second;
 }
 
 void MFEngine::plan() {
@@ -328,6 +359,13 @@ void MFEngine::plan() {
         m.u[0] = c.u0.as<float>();
         m.u[1] = c.u1.as<float>();
         m.rhs = c.rhs.as<float>();
+        if (s0.spec.kind == MF_KIND_WAVE && !s0.spec.apply && wave_square_levels() > 0) {
+            const QTable& Q = qtab(s0.spec.k, s0.spec.n);
+            m.q_rowptr = Q.rowptr.as<int32_t>();
+            m.q_ent = Q.ent.as<int32_t>();
+            m.q_val = Q.val.as<float>();
+            for (size_t l = 0; l < Q.roff.size(); l++) m.q_roff[l] = Q.roff[l];
+        }
         m.dt = c.dt.as<double>();
         m.coef = c.coef.as<float>();
         m.status = c.status.as<int32_t>();
@@ -435,9 +473,14 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                     const int Wp = mf_tile_cols(k, cpt, nrb, tile.wlog);
                     const int64_t cbeg = (int64_t)s0 * p.R, cend = (int64_t)s1 * p.R;
                     smem = std::max(smem, mf_tile_smem(k, nrb, Wp));
+                    // the wave steps short lines with the squared table
+                    const int ptab = tab == TABLE_DERIVATIVE && sp.kind == MF_KIND_WAVE && !sp.apply &&
+                                             p.lmax <= wave_square_levels()
+                                         ? TABLE_SQUARE
+                                         : tab;
                     for (int64_t g0 = cbeg; g0 < cend; g0 += Wp) {
                         MFItem it{};
-                        it.tab = (int16_t)tab;
+                        it.tab = (int16_t)ptab;
                         it.cls = (int16_t)ci;
                         it.d = (int16_t)d;
                         it.flags = (int16_t)flags;

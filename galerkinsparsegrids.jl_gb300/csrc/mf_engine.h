@@ -87,6 +87,10 @@ class MFEngine {
     struct TTables {  // the four nodal transforms of one (k, n)
         STable t[4];
     };
+    struct QTable {  // the squared line operators of one (k, n)
+        DevBuf rowptr, ent, val;
+        std::vector<int32_t> roff;
+    };
     struct ClassArena {
         std::tuple<int, int, int, int, int, bool, int> key;
         SparseIndex ix;
@@ -106,6 +110,7 @@ class MFEngine {
                      std::vector<std::array<int, 3>>* ranges = nullptr);
     const STable& stab(int k, int n);
     const TTables& ttab(int k, int n);
+    const QTable& qtab(int k, int n);
     void capture();
     void drop_graph();
     Solve& at(int id);
@@ -116,6 +121,7 @@ class MFEngine {
     std::vector<std::unique_ptr<ClassArena>> classes_;
     std::map<std::pair<int, int>, STable> stabs_;
     std::map<std::pair<int, int>, TTables> ttabs_;
+    std::map<std::pair<int, int>, QTable> qtabs_;
     DevBuf classes_d_, items_d_, ctr_d_, err_d_;
     int nitems_ = 0, nctr_ = 0, grid_ = 0, sms_ = 0;  // grid_: resident CTAs per SM x SMs
     int64_t pending_bytes_ = 0;  // admitted but not yet allocated

@@ -85,6 +85,18 @@ struct MFOperator {
     std::vector<float> val;       // ndist blocks of k rows x rs floats
 };
 MFOperator mf_operator(int k, int n);                  // the 1D derivative, pruned
+// The squared line operators B B (B = leading block of the pruned 1D
+// operator for line length lm = 1..n+1), one block-CSR table per lm: row
+// pointers of lm at rowptr[roff[lm - 1] ..], entries as in MFOperator, the
+// distinct blocks shared by all lm.
+struct MFSquareTables {
+    int k = 0, n = 0, rs = 0, ndist = 0;
+    std::vector<int32_t> roff;    // n + 1
+    std::vector<int32_t> rowptr;  // sum over lm of 2^(lm-1) + 1
+    std::vector<int32_t> ent;
+    std::vector<float> val;
+};
+MFSquareTables mf_square_tables(int k, int n);
 MFOperator mf_transform_table(int k, int n, int which);  // a nodal transform (see below)
 
 // ------------------------------------------------------------ index map ----
