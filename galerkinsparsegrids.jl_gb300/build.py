@@ -11,12 +11,18 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-OUT = os.path.join(HERE, "_build")
+# SGDG_DEBUG=1 builds (and the package then loads) the debug library, with
+# device index checks, into its own directory
+DEBUG = os.environ.get("SGDG_DEBUG") == "1"
+OUT = os.path.join(HERE, "_build_debug" if DEBUG else "_build")
 LIB = os.path.join(OUT, "libsgdg.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off"]
+if DEBUG:
+    HOST_FLAGS = HOST_FLAGS + ["-DSGDG_DEBUG"]
+    NVCC_FLAGS = NVCC_FLAGS + ["-DSGDG_DEBUG"]
 
 
 def _nvcc():
@@ -36,7 +42,7 @@ def _digest():
     h = hashlib.sha256()
     for d in (CSRC, INCLUDE):
         for f in sorted(os.listdir(d)):
-            if f.endswith((".cpp", ".cu", ".h")):
+            if f.endswith((".cpp", ".cu", ".h", ".cuh")):
                 with open(os.path.join(d, f), "rb") as fh:
                     h.update(f.encode() + fh.read())
     h.update(" ".join(ARCH + HOST_FLAGS + NVCC_FLAGS).encode())

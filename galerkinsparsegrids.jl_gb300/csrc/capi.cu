@@ -20,6 +20,9 @@
 namespace sgdg {
 
 cudaError_t launch_csr_spmv(const DevCSR& A, const double* x, double* y, cudaStream_t st);
+cudaError_t mf_bounds_violations(unsigned int* out, bool reset);
+cudaError_t csr_bounds_violations(unsigned int* out, bool reset);
+cudaError_t asm_bounds_violations(unsigned int* out, bool reset);
 cudaError_t launch_csr_rk4_batch(const DevCSR& A, int64_t nb, int64_t bs, const double* uin, double* y, double* acc,
                                  double* uout, double dt, int stage, cudaStream_t st);
 cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double* acc, double* uout, double dt,
@@ -581,6 +584,26 @@ int sgdg_op_plain_steps_device(sgdg_op* op, int which, int64_t nsolves, double* 
     if (!std::isfinite(dt)) throw Error(SGDG_EINVAL, "dt must be finite");
     require_gpu();
     if (nsteps > 0) plain_batch_steps(op, which, nsolves, y_dev, dt, nsteps, (cudaStream_t)stream);
+    API_END
+}
+
+int sgdg_debug_bounds(int* checked, int64_t* violations, int reset) {
+    API_BEGIN
+    NEED(checked);
+    NEED(violations);
+    *violations = 0;
+#ifdef SGDG_DEBUG
+    *checked = 1;
+#else
+    *checked = 0;
+    return SGDG_OK;  // nothing is checked (or counted) in this build
+#endif
+    require_gpu();
+    unsigned int v = 0;
+    for (auto f : {mf_bounds_violations, csr_bounds_violations, asm_bounds_violations}) {
+        CK(f(&v, reset != 0));
+        *violations += v;
+    }
     API_END
 }
 

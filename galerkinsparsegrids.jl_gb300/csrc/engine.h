@@ -81,6 +81,7 @@ struct MFClass {
     const float* coef;        // per slot, 16 entries: factor on D_d as hi[8], lo[8]
     const int32_t* status;    // per slot, nonzero = skip the RK update
     int32_t N, Ns;
+    int32_t nslots;           // slots of the arenas
     int32_t D, k, kD, kind, rs;
     int32_t s_nrow, s_nent, s_nval;  // table sizes (ints, ints, floats) for the shared-memory copy
     int32_t s_shared;                // 1: pass tiles read a shared-memory copy of the table; 0: global memory

@@ -21,6 +21,7 @@
 #include <climits>
 
 #include "../../include/sgdg.h"
+#include "bounds.cuh"
 #include "device_csr.h"
 
 namespace sgdg {
@@ -71,7 +72,8 @@ __global__ void k_line_count(LineArgs A, int32_t* rowlen) {
     const PencilDesc pd = A.pen[P];
     const int2 ri = A.rows[pd.roff + row];
     const int64_t* rp = A.trowptr + A.troff[pd.lmax - 1];
-    rowlen[ri.x + a + (b << ri.y)] = (int32_t)(rp[row + 1] - rp[row]);
+    const int64_t i = ri.x + a + ((int64_t)b << ri.y);
+    if (SGDG_IN(i, A.N)) rowlen[i] = (int32_t)(rp[row + 1] - rp[row]);
 }
 
 __global__ void k_line_fill(LineArgs A, const int64_t* __restrict__ rowptr, int32_t* __restrict__ col,
@@ -83,10 +85,14 @@ __global__ void k_line_fill(LineArgs A, const int64_t* __restrict__ rowptr, int3
     const PencilDesc pd = A.pen[P];
     const int2 ri = A.rows[pd.roff + row];
     const int64_t* rp = A.trowptr + A.troff[pd.lmax - 1];
-    int64_t w = rowptr[ri.x + a + (b << ri.y)];
+    const int64_t i = ri.x + a + ((int64_t)b << ri.y);
+    if (!SGDG_IN(i, A.N)) return;
+    int64_t w = rowptr[i];
     for (int64_t t = rp[row]; t < rp[row + 1]; t++, w++) {
         const int2 rq = A.rows[pd.roff + A.tcol[t]];
-        col[w] = rq.x + a + (b << rq.y);
+        const int64_t c = rq.x + a + ((int64_t)b << rq.y);
+        if (!SGDG_IN(w - rowptr[i], rowptr[i + 1] - rowptr[i]) || !SGDG_IN(c, A.N)) continue;
+        col[w] = (int32_t)c;
         val[w] = A.tval[t];
     }
 }
@@ -131,7 +137,7 @@ __global__ void k_sum(SumArgs A, int32_t* rowlen, const int64_t* __restrict__ ro
             v = __dadd_rn(v, x);
         }
         if (v == 0.0) continue;  // map(+) drops sums that are exactly 0.0
-        if (FILL) {
+        if (FILL && SGDG_IN(w, rowptr[i + 1])) {
             col[w] = c;
             val[w] = v;
             w++;
@@ -340,6 +346,7 @@ __device__ int32_t tuple_entries(const TransArgs& A, const int* g, const int (*g
                 if (v == 0.0) break;
             }
             if (!(fabs(v) < 1e-12)) {
+                if (FILL && !(w + cnt < lim)) (void)SGDG_IN(w + cnt, lim);  // debug build: counted
                 if (FILL && w + cnt < lim) {
                     int64_t mode_lin = 0, ms = 1;
                     for (int d = 0; d < D; d++) {
@@ -640,6 +647,8 @@ std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, c
     finish_device_csr(*R, rph, ix.N, st);
     return R;
 }
+
+SGDG_BOUNDS_READER(asm_bounds_violations)
 
 std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st) {
     require_gpu();

@@ -21,6 +21,7 @@
 
 #include <cstdint>
 
+#include "bounds.cuh"
 #include "engine.h"
 #include "rk.cuh"
 
@@ -132,8 +133,12 @@ __device__ __forceinline__ void csr_row(const DevCSR& A, int64_t row, const doub
         int64_t p = b + lane;
         // four entries per lane in flight: the column loads, then the gathers of x
         for (; p + 3 * VS < e; p += 4 * VS) {
-            const int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + VS), c2 = __ldg(A.col + p + 2 * VS),
-                      c3 = __ldg(A.col + p + 3 * VS);
+            int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + VS), c2 = __ldg(A.col + p + 2 * VS),
+                c3 = __ldg(A.col + p + 3 * VS);
+            if (!SGDG_IN(c0, A.m)) c0 = 0;  // debug build: counted, read column 0 instead
+            if (!SGDG_IN(c1, A.m)) c1 = 0;
+            if (!SGDG_IN(c2, A.m)) c2 = 0;
+            if (!SGDG_IN(c3, A.m)) c3 = 0;
             const double v0 = __ldg(A.val + p), v1 = __ldg(A.val + p + VS), v2 = __ldg(A.val + p + 2 * VS),
                          v3 = __ldg(A.val + p + 3 * VS);
             double x0[NV], x1[NV], x2[NV], x3[NV];
@@ -150,7 +155,8 @@ __device__ __forceinline__ void csr_row(const DevCSR& A, int64_t row, const doub
             }
         }
         for (; p < e; p += VS) {
-            const int c = __ldg(A.col + p);
+            int c = __ldg(A.col + p);
+            if (!SGDG_IN(c, A.m)) c = 0;
             const double v = __ldg(A.val + p);
             double xv[NV];
             csr_gather<NV, W>(x, c * xi, xs, xv);
@@ -179,7 +185,8 @@ __device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, const double* 
     const int64_t t = (int64_t)(blockIdx.x - A.bin_block[bin]) * blockDim.x + threadIdx.x;
     const int64_t idx = t / VS, first = A.bin_first[bin];
     const int lane = int(t % VS);
-    const int64_t row = idx < A.bin_first[bin + 1] - first ? (int64_t)A.bin_rows[first + idx] : -1;
+    int64_t row = idx < A.bin_first[bin + 1] - first ? (int64_t)A.bin_rows[first + idx] : -1;
+    if (row >= 0 && !SGDG_IN(row, A.m)) row = -1;
     double s[NV];
     csr_row<VS, NV, W>(A, row, x, xi, xs, lane, s);
     bool stores;
@@ -234,8 +241,11 @@ __global__ void __launch_bounds__(256) k_csr_segments(DevCSR A, const double* __
     const int64_t e = A.seg_end[seg];
     int64_t p = A.seg_begin[seg] + lane;
     for (; p + 96 < e; p += 128) {
-        const int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + 32), c2 = __ldg(A.col + p + 64),
-                  c3 = __ldg(A.col + p + 96);
+        int c0 = __ldg(A.col + p), c1 = __ldg(A.col + p + 32), c2 = __ldg(A.col + p + 64), c3 = __ldg(A.col + p + 96);
+        if (!SGDG_IN(c0, A.m)) c0 = 0;
+        if (!SGDG_IN(c1, A.m)) c1 = 0;
+        if (!SGDG_IN(c2, A.m)) c2 = 0;
+        if (!SGDG_IN(c3, A.m)) c3 = 0;
         const double v0 = __ldg(A.val + p), v1 = __ldg(A.val + p + 32), v2 = __ldg(A.val + p + 64),
                      v3 = __ldg(A.val + p + 96);
         double x0[NV], x1[NV], x2[NV], x3[NV];
@@ -252,7 +262,8 @@ __global__ void __launch_bounds__(256) k_csr_segments(DevCSR A, const double* __
         }
     }
     for (; p < e; p += 32) {
-        const int c = __ldg(A.col + p);
+        int c = __ldg(A.col + p);
+        if (!SGDG_IN(c, A.m)) c = 0;
         const double v = __ldg(A.val + p);
         double xv[NV];
         csr_gather<NV, W>(x, c * xi, xs, xv);
@@ -282,6 +293,7 @@ __global__ void k_csr_long_rows(DevCSR A, int nv, double* y, int64_t yi, int64_t
     double s = 0.0;
     for (int q = A.long_seg[i]; q < A.long_seg[i + 1]; q++) s += A.partial[j * A.nseg + q];
     const int64_t row = A.long_row[i];
+    if (!SGDG_IN(row, A.m)) return;
     if (rk_on)
         csr_rk_update(rk, row, s, y);
     else
@@ -315,6 +327,8 @@ __global__ void k_vlasov_points(const double* __restrict__ v, const double* __re
         out[i] = __dadd_rn(-c1, c2);
     }
 }
+
+SGDG_BOUNDS_READER(csr_bounds_violations)
 
 // ------------------------------------------------------------ launchers ----
 static int grid_for(int64_t threads) {

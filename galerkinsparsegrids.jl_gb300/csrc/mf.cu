@@ -28,6 +28,7 @@
 #include <map>
 #include <mutex>
 
+#include "bounds.cuh"
 #include "engine.h"
 #include "cvt.cuh"
 #include "rk.cuh"
@@ -210,7 +211,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const int slot = div_invariant(g, it.rmagic, it.rshift), r = g - slot * R;
             const int cr = div_pow<K>(r, C.D - 1), mr = r - cr * kDm1;
             const int mq = div_pow<K>(mr, it.d);
-            cslot[j] = slot;
+            cslot[j] = SGDG_IN(slot, C.nslots) ? slot : -1;
             ca[j] = kD * (cr & ((1 << lp) - 1)) + (mr - mq * kd1) + mq * kd1 * K;
             cb[j] = kD * ((cr >> lp) << lp);
         } else {
@@ -243,7 +244,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const int bj = cb[j];
             for (int row = r0; row < m; row += rstep) {
                 const int2 ri = rinfo[row];
-                cp_async4(xc + row * W, base + ri.x + (bj << ri.y));
+                const int o = ri.x + (bj << ri.y);
+                if (SGDG_IN(ca[j] + o, C.N))
+                    cp_async4(xc + row * W, base + o);
+                else
+                    xc[row * W] = 0.f;
             }
         });
         cp_async_wait_all();
@@ -263,7 +268,12 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const size_t step2 = 2 * (size_t)C.vstride;
             for (int row = r0; row < m; row += rstep) {
                 const int2 ri = rinfo[row];
-                const float* p = base + ri.x + (bj << ri.y);
+                const int o = ri.x + (bj << ri.y);
+                if (!SGDG_IN(ca[j] + o, C.N)) {
+                    xc[row * W] = 0.f;
+                    continue;
+                }
+                const float* p = base + o;
                 float v = __ldcg(p);
                 for (int q = 1; q < nsum; q++) v += __ldcg(p + q * step2);  // the D products, in order
                 xc[row * W] = v;
@@ -319,12 +329,15 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const int bj = cb[j];
             for (int row0 = r0; row0 < m; row0 += kOutRows * rstep) {
                 int off[kOutRows];
+                bool bad[kOutRows];
                 float v[kOutRows], wh[kOutRows], wl[kOutRows], prev[kOutRows];
 #pragma unroll
                 for (int u = 0; u < kOutRows; u++) {
                     const int row = min(row0 + u * rstep, m - 1);
                     const int2 ri = rinfo[row];
                     off[u] = ri.x + (bj << ri.y);
+                    bad[u] = !SGDG_IN(ca[j] + off[u], C.N);
+                    if (bad[u]) off[u] = -ca[j];  // loads the slot's first element, stores nothing
                     v[u] = Z[row * W + j];
                     wh[u] = wacc ? __ldg(wc + off[u]) : 0.f;
                     wl[u] = wacc ? __ldg(wc + wlo + off[u]) : 0.f;
@@ -333,6 +346,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
 #pragma unroll
                 for (int u = 0; u < kOutRows; u++) {
                     if (row0 + u * rstep >= m) break;
+                    if (bad[u]) continue;
                     float x = v[u];
                     if (wacc) {
                         x = fmaf(wh[u], x, wl[u] * x);
@@ -352,18 +366,22 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const int bj = cb[j];
             for (int row0 = r0; row0 < m; row0 += kOutRows * rstep) {
                 int off[kOutRows];
+                bool bad[kOutRows];
                 float z[kOutRows], prev[kOutRows];
 #pragma unroll
                 for (int u = 0; u < kOutRows; u++) {
                     const int row = min(row0 + u * rstep, m - 1);
                     const int2 ri = rinfo[row];
                     off[u] = ri.x + (bj << ri.y);
+                    bad[u] = !SGDG_IN(ca[j] + off[u], C.N);
+                    if (bad[u]) off[u] = -ca[j];  // loads the slot's first element, stores nothing
                     z[u] = Z[row * W + j];
                     prev[u] = first ? 0.f : __ldcg(rc + off[u]);
                 }
 #pragma unroll
                 for (int u = 0; u < kOutRows; u++) {
                     if (row0 + u * rstep >= m) break;
+                    if (bad[u]) continue;
                     float v = fmaf(chi, z[u], clo * z[u]);
                     if (!first) v += prev[u];
                     __stcg(rc + off[u], v);
@@ -389,6 +407,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         const int bj = cb[j];
         for (int row0 = r0; row0 < m; row0 += R_ * rstep) {
             int off[R_];
+            bool bad[R_];
             float z[R_], prev[R_], kf[R_];
             double yv[R_], av[R_], yf[R_], af[R_];
 #pragma unroll
@@ -396,6 +415,8 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
                 const int row = min(row0 + u * rstep, m - 1);
                 const int2 ri = rinfo[row];
                 off[u] = ri.x + (bj << ri.y);
+                bad[u] = !SGDG_IN(ca[j] + off[u], C.N);
+                if (bad[u]) off[u] = -ca[j];  // loads the slot's first element, stores nothing
                 z[u] = Z[row * W + j];
             }
 #pragma unroll
@@ -412,6 +433,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
 #pragma unroll
             for (int u = 0; u < R_; u++) {
                 if (row0 + u * rstep >= m) break;
+                if (bad[u]) continue;
                 const int o = off[u];
                 float v = fmaf(chi, z[u], clo * z[u]);
                 if (!first) v += prev[u];
@@ -561,6 +583,8 @@ cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* clas
 // for the whole process, and every engine (and the allocation-free entry
 // point) launches with the size it planned: so the limit only ever rises,
 // to the largest size any caller has asked for on that device.
+SGDG_BOUNDS_READER(mf_bounds_violations)
+
 cudaError_t mf_configure(size_t smem, int* blocks_per_sm) {
     static std::mutex mu;
     static std::map<int, size_t> limit;  // device -> attribute value set

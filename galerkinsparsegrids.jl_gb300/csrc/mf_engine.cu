@@ -371,6 +371,7 @@ void MFEngine::plan() {
         m.status = c.status.as<int32_t>();
         m.N = (int32_t)c.N;
         m.Ns = (int32_t)c.Ns;
+        m.nslots = (int32_t)c.slots.size();
         m.D = s0.spec.D;
         m.k = s0.spec.k;
         int kD = 1;

@@ -230,6 +230,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         c.status = reinterpret_cast<const int32_t*>(base + r_status.off);
         c.N = N;
         c.Ns = N;
+        c.nslots = 1;
         c.D = D;
         c.k = k;
         c.kD = (int)ix.kD;

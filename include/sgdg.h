@@ -115,6 +115,15 @@ int sgdg_apply_device(sgdg_op *op, int which, int method, const double *x_dev, d
 int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, const double *x_dev, double *y_dev,
                        void *stream);
 
+/* Device index checks of a debug build (built with SGDG_DEBUG=1): every
+ * gather and scatter index of the matrix-free, CSR and assembly kernels is
+ * checked against its vector's length, and a failed check is counted and its
+ * access skipped instead of trapping.  *checked = 1 in a debug build (0
+ * otherwise, with *violations = 0); *violations = failed checks since the
+ * last reset (reset != 0 clears them).  No counterpart in the reference:
+ * it stands in for a memory checker on GPUs where none can run. */
+int sgdg_debug_bounds(int *checked, int64_t *violations, int reset);
+
 /* ---- evolvers ----------------------------------------------------------- */
 /* wave_evolve (src/pdes.jl:54-70) with classical RK4 and nsteps fixed steps on
  * [t0, t1]: u_tt = laplacian(u), state [f; v].  Writes nout >= 2 equally

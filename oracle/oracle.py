@@ -365,10 +365,13 @@ def vlasov_rhs(D, k, n, ops, F_point, f):
     operators ``ops`` = (Ds (2D CSR), m2n, n2p, p2n, n2m) and the velocity
     points v_point built as in src/pdes.jl:166-172."""
     Ds, m2n, n2p, p2n, n2m, v_point = ops
-    dfdx = [Ds[d] @ f for d in range(D)]
-    dfdp = [Ds[d] @ f for d in range(D, 2 * D)]
-    xpt = [n2p @ (m2n @ x) for x in dfdx]
-    ppt = [n2p @ (m2n @ x) for x in dfdp]
+    # the 2D derivatives go through m2n and n2p as the columns of one block
+    # (scipy sums each column's row in the same order as a single SpMV, so
+    # the values are those of separate products; the matrix is read once)
+    grads = np.column_stack([Ds[d] @ f for d in range(2 * D)])
+    pts = n2p @ (m2n @ grads)
+    xpt = [pts[:, d] for d in range(D)]
+    ppt = [pts[:, D + d] for d in range(D)]
     c1 = sum(v_point[d] * xpt[d] for d in range(D))
     c2 = sum(F_point[d] * ppt[d] for d in range(D))
     return n2m @ (p2n @ (-c1 + c2))

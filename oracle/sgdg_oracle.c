@@ -1393,10 +1393,18 @@ or_mat *or_transform(int D, int k, int n, int scheme, const or_mat *T1) {
     for (int64_t j = 0; j < T1->n; j++)
         for (int64_t p = T1->colptr[j]; p < T1->colptr[j + 1]; p++) M1[T1->rowval[p] * len + j] = T1->nzval[p];
     const double atol = 1e-12;
-    coo_t co = {0};
-    int L1[16], C1[16], Mo1[16], L2[16], C2[16], Mo2[16];
-    int64_t j = 0;
+    /* Columns of one level tuple t1 are the contiguous run starting at
+     * lev_off[t1]; each tuple's entries go to their own list (in the
+     * sequential order), and the lists are joined in tuple order, so the
+     * COO sequence -- and the assembled matrix -- is the sequential one. */
+    coo_t *parts = calloc((size_t)ix.nlev, sizeof(coo_t));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
     for (int t1 = 0; t1 < ix.nlev; t1++) {
+        coo_t *co = &parts[t1];
+        int L1[16], C1[16], Mo1[16], L2[16], C2[16], Mo2[16];
+        int64_t j = ix.lev_off[t1];
         for (int q = 0; q < D; q++) L1[q] = ix.levels[t1 * D + q];
         int64_t cells1 = 1;
         for (int q = 0; q < D; q++) cells1 *= ncells_of(L1[q]);
@@ -1441,7 +1449,7 @@ or_mat *or_transform(int D, int k, int n, int scheme, const or_mat *T1) {
                                 val *= M1[(int64_t)i1 * len + js[q]];
                                 if (val == 0) break;
                             }
-                            if (!(fabs(val) < atol)) coo_push(&co, i, j, val);
+                            if (!(fabs(val) < atol)) coo_push(co, i, j, val);
                             i++;
                         }
                     }
@@ -1450,6 +1458,12 @@ or_mat *or_transform(int D, int k, int n, int scheme, const or_mat *T1) {
             }
         }
     }
+    coo_t co = {0};
+    for (int t1 = 0; t1 < ix.nlev; t1++) {
+        for (int64_t e = 0; e < parts[t1].len; e++) coo_push(&co, parts[t1].I[e], parts[t1].J[e], parts[t1].V[e]);
+        coo_free(&parts[t1]);
+    }
+    free(parts);
     free(M1);
     or_mat *R = coo_to_csc(ix.N, ix.N, &co);
     coo_free(&co);
