@@ -307,7 +307,16 @@ def vlasov_leg(sg, stream, steps, batch=16):
     b.autotune()
     ms_b = timed_steps(b, stream, 20, 3)
     b.close()
-    out["matfree_batch"] = {"solves": batch, "value": batch * N * 4.0 / (ms_b / 1e3), "ms_per_step": ms_b}
+    rate = batch * N * 4.0 / (ms_b / 1e3)
+    # algorithmic bytes per DOF-update: the RK state's 32 B (as for the wave)
+    # and the point weights of the 2 Dx products, an FP32 hi/lo pair each
+    bpd = BYTES_PER_DOF_UPDATE + 2 * (2 * Dx) * 4.0
+    peak, peak_kind = measured_peak_hbm()
+    out["matfree_batch"] = {"solves": batch, "value": rate, "ms_per_step": ms_b,
+                            "roofline": {"bound": "hbm", "achieved": rate * bpd / 1e9, "peak": peak, "unit": "GB/s",
+                                         "frac": rate * bpd / 1e9 / peak, "peak_kind": peak_kind,
+                                         "bytes_per_dof_update": bpd,
+                                         "working_set_bytes": int(batch * N * (24 + 4 + 4 * 4 * (2 * Dx)))}}
     return out
 
 

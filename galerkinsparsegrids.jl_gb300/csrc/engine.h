@@ -87,6 +87,7 @@ struct MFClass {
     int32_t s_shared;                // 1: pass tiles read a shared-memory copy of the table; 0: global memory
     // Vlasov classes: the four nodal transforms (1D block tables, read through
     // L1), scratch vectors and the point weights of the D point products
+    int32_t t_nrow[4], t_nent[4], t_nval[4];  // their sizes, as s_nrow, s_nent, s_nval
     const int32_t* t_rowptr[4];
     const int32_t* t_ent[4];
     const float* t_val[4];
@@ -96,6 +97,9 @@ struct MFClass {
 };
 
 // bytes of the shared-memory copy of a class's 1D operator table
+#ifdef __CUDACC__
+__host__ __device__
+#endif
 inline int mf_table_bytes(int nrow, int nent, int nval) {
     return (((nrow + nent) * 4 + 15) / 16) * 16 + nval * 4;
 }

@@ -512,22 +512,34 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             s_cls_id = it.cls;  // read again only after the next barrier
             done = it.done_ctr;
         }
+        // the item's table: the derivative table or a nodal transform (a
+        // shared-memory copy when it fits the reserved space, cached across
+        // items by its row pointers), or the wave's squared line operators
+        // (through L1)
         OpTable T{C.s_rowptr, C.s_ent, C.s_val};
-        if (it.tab == TABLE_SQUARE) {  // the wave's squared line operator: read through L1
+        int tn[3] = {C.s_nrow, C.s_nent, C.s_nval};
+        bool tsh = C.s_shared != 0;
+        if (it.tab == TABLE_SQUARE) {
             T = OpTable{C.q_rowptr + C.q_roff[it.lmax - 1], C.q_ent, C.q_val};
-        } else if (it.tab != TABLE_DERIVATIVE) {  // a nodal transform: read through L1
+            tsh = false;
+        } else if (it.tab != TABLE_DERIVATIVE) {
             T = OpTable{C.t_rowptr[it.tab], C.t_ent[it.tab], C.t_val[it.tab]};
-        } else if (C.s_shared) {
+            tn[0] = C.t_nrow[it.tab];
+            tn[1] = C.t_nent[it.tab];
+            tn[2] = C.t_nval[it.tab];
+            tsh = mf_table_bytes(tn[0], tn[1], tn[2]) <= table_bytes;
+        }
+        if (tsh) {
             int* trow = reinterpret_cast<int*>(smem);
-            int* tent = trow + C.s_nrow;
-            float* tval = smem + (((C.s_nrow + C.s_nent) * 4 + 15) / 16) * 4;
-            if (s_cached != C.s_rowptr) {  // copy the operator table (uniform branch; classes of one (k, n) share it)
-                for (int i = tid; i < C.s_nrow; i += kMFThreads) trow[i] = C.s_rowptr[i];
-                for (int i = tid; i < C.s_nent; i += kMFThreads) tent[i] = C.s_ent[i];
-                for (int i = tid; i < C.s_nval / 4; i += kMFThreads)
-                    reinterpret_cast<float4*>(tval)[i] = reinterpret_cast<const float4*>(C.s_val)[i];
+            int* tent = trow + tn[0];
+            float* tval = smem + (((tn[0] + tn[1]) * 4 + 15) / 16) * 4;
+            if (s_cached != T.rowptr) {  // copy the table (uniform branch; classes of one (k, n) share it)
+                for (int i = tid; i < tn[0]; i += kMFThreads) trow[i] = T.rowptr[i];
+                for (int i = tid; i < tn[1]; i += kMFThreads) tent[i] = T.ent[i];
+                for (int i = tid; i < tn[2] / 4; i += kMFThreads)
+                    reinterpret_cast<float4*>(tval)[i] = reinterpret_cast<const float4*>(T.val)[i];
                 __syncthreads();
-                if (tid == 0) s_cached = C.s_rowptr;
+                if (tid == 0) s_cached = T.rowptr;
             }
             T = OpTable{trow, tent, tval};
         }

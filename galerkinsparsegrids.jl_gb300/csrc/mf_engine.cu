@@ -383,6 +383,9 @@ void MFEngine::plan() {
             const TTables& T = ttab(m.k, s0.spec.n);
             for (int w = 0; w < 4; w++) {
                 m.t_rowptr[w] = T.t[w].rowptr.as<int32_t>();
+                m.t_nrow[w] = T.t[w].nrow;
+                m.t_nent[w] = T.t[w].nent;
+                m.t_nval[w] = T.t[w].nval;
                 m.t_ent[w] = T.t[w].ent.as<int32_t>();
                 m.t_val[w] = T.t[w].val.as<float>();
             }
@@ -603,6 +606,13 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
         const STable& S = stab(sp.k, sp.n);
         const int b = mf_table_bytes(S.nrow, S.nent, S.nval);
         if (b <= kMFTableSmemMax) tb = std::max(tb, b);
+        if (sp.kind == MF_KIND_VLASOV) {  // the transforms share the slot, one at a time
+            const TTables& T = ttab(sp.k, sp.n);
+            for (int w = 0; w < 4; w++) {
+                const int bt = mf_table_bytes(T.t[w].nrow, T.t[w].nent, T.t[w].nval);
+                if (bt <= kMFTableSmemMax) tb = std::max(tb, bt);
+            }
+        }
     }
     table_bytes_ = tb;
     smem += (size_t)tb;
