@@ -143,14 +143,19 @@ def vcoeffs_1d(k, n, f, q=None):
     return np.concatenate(res)
 
 
-def vcoeffs_DG(D, k, n, f, scheme="sparse", q=None):
+def vcoeffs_DG(D, k, n, f, scheme="sparse", q=None, device=False):
     """Coefficient vector of f (src/dg_vmethods.jl:149-179).
 
     ``f`` takes an (npts, D) array of points and returns npts values.  The
     reference integrates each basis function with hcubature; here every level
     block is integrated at once with tensor Gauss-Legendre rules on the
-    polynomial pieces (exact for polynomials of degree < 2q)."""
+    polynomial pieces (exact for polynomials of degree < 2q).  With
+    ``device=True`` f is sampled on the host at every block's tensor grid of
+    nodes and the GPU contracts the samples dimension by dimension
+    (sgdg_vcoeffs_contract)."""
     q = q or max(6, k + 3)
+    if device:
+        return _vcoeffs_device(D, k, n, f, scheme, q)
     if D == 1:
         return vcoeffs_1d(k, n, lambda x: np.asarray(f(x.reshape(-1, 1)), np.float64).reshape(x.shape), q)
     pieces = _pieces_1d(k, n, q)
@@ -184,6 +189,27 @@ def vcoeffs_DG(D, k, n, f, scheme="sparse", q=None):
         # axes (c1, m1, ..., cD, mD) -> reference order: cells (dim 1 fastest) then modes (dim 1 fastest)
         order = [2 * q for q in reversed(range(D))] + [2 * q + 1 for q in reversed(range(D))]
         out[pos:pos + size] = np.transpose(F, order).ravel()
+    return out
+
+
+def _vcoeffs_device(D, k, n, f, scheme, q):
+    pieces = _pieces_1d(k, n, q)
+    npts = np.array([nodes.shape[1] for nodes, _, _ in pieces], np.int32)
+    wtab = np.concatenate([(vals * wts[None, None, :]).ravel() for _, wts, vals in pieces])
+    L, _, _ = index_map(D, k, n, scheme)
+    N = L.shape[0]
+    samples = []
+    pos = 0
+    while pos < N:
+        lv = tuple(int(v) for v in L[pos])
+        nodes = [pieces[l - 1][0].ravel() for l in lv]  # dimension q: cell * P + node
+        grids = np.meshgrid(*nodes[::-1], indexing="ij")  # last axis (dimension 1) fastest
+        pts = np.stack([g.ravel() for g in grids[::-1]], axis=1)
+        samples.append(np.asarray(f(pts), np.float64).reshape(-1))
+        pos += int(np.prod([1 << max(0, l - 2) for l in lv])) * k ** D
+    out = np.empty(N)
+    check(lib().sgdg_vcoeffs_contract(D, k, n, _scheme(scheme), npts, np.ascontiguousarray(wtab),
+                                      np.ascontiguousarray(np.concatenate(samples)), out))
     return out
 
 

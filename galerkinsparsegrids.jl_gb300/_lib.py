@@ -19,7 +19,7 @@ EXPORTS = [
     "sgdg_version", "sgdg_last_error", "sgdg_get_size", "sgdg_index_map", "sgdg_dg_coeffs", "sgdg_dlf_1d_nnz",
     "sgdg_dlf_1d_export", "sgdg_op_create", "sgdg_op_destroy", "sgdg_op_size", "sgdg_op_nnz",
     "sgdg_op_export_csr", "sgdg_op_device_nnz", "sgdg_op_export_device_csr", "sgdg_apply", "sgdg_apply_device", "sgdg_apply_noalloc", "sgdg_wave_evolve",
-    "sgdg_advect_evolve", "sgdg_op_plain_steps_device", "sgdg_debug_bounds",
+    "sgdg_advect_evolve", "sgdg_op_plain_steps_device", "sgdg_debug_bounds", "sgdg_vcoeffs_contract",
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
     "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_host", "sgdg_batch_step_info", "sgdg_batch_autotune",
@@ -91,6 +91,7 @@ def lib(build=True):
     _sig(L, "sgdg_advect_evolve", [_vp, _f64p, _f64p, _cd, _cd, _c64, _ci, _ci, _f64p, _f64p])
     _sig(L, "sgdg_op_plain_steps_device", [_vp, _ci, _c64, _vp, _cd, _c64, _vp])
     _sig(L, "sgdg_debug_bounds", [ctypes.POINTER(_ci), ctypes.POINTER(_c64), _ci])
+    _sig(L, "sgdg_vcoeffs_contract", [_ci, _ci, _ci, _ci, _i32p, _f64p, _f64p, _f64p])
     _sig(L, "sgdg_transform_1d_nnz", [_ci, _ci, _ci, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_transform_1d_export", [_ci, _ci, _ci, _i64p, _i32p, _f64p])
     _sig(L, "sgdg_transform_nnz", [_ci, _ci, _ci, _ci, _ci, ctypes.POINTER(_c64)])

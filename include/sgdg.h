@@ -307,6 +307,17 @@ int sgdg_server_counts(sgdg_server *s, int64_t *queued, int64_t *running, int64_
  * functions vanish there. */
 int sgdg_evaluate(int D, int k, int n, int scheme, const double *coeffs, int64_t npts, const double *xs,
                   double *values);
+/* vcoeffs_DG (src/dg_vmethods.jl:149-179) on the GPU for a function the
+ * caller samples: every level block is integrated by tensor quadrature on
+ * its 1D pieces.  npts[L-1] = quadrature nodes per cell of level L = 1..n+1;
+ * wtab = for each L in turn, cells_L x k x npts[L-1] values (basis function
+ * (cell, mode) at each node times its weight); samples = f at every block's
+ * tensor grid of nodes, blocks in coefficient order, each block's grid with
+ * dimension 1 fastest and, per dimension, node index cell * npts + node.
+ * out = the N coefficients in the reference's order (host buffers). */
+int sgdg_vcoeffs_contract(int D, int k, int n, int scheme, const int32_t *npts, const double *wtab,
+                          const double *samples, double *out);
+
 /* Sum of separable terms, computed on the GPU: coefficient i of the D-dim
  * vector is sum_t amp_t * part_t(e^{i phi_t} prod_d Z_td[i_d]) with i_d the
  * 1D index of i along d (get_index_1D, src/additional_tools.jl:8-13).  Z holds

@@ -32,3 +32,30 @@ def test_fourier_device_matches_host(sgdg, D, k, n):
 def test_tensor_sum_argument_checks(sgdg):
     with pytest.raises(ValueError):
         sgdg._tensor_sum(2, 2, 3, np.zeros((1, 3, 16)), [[1, 1, 0, 0]], "sparse")
+
+
+# vcoeffs_DG (src/dg_vmethods.jl:149-179) of a general (non-separable) f:
+# host samples at the quadrature nodes, GPU contraction over the level blocks
+# (sgdg_vcoeffs_contract); the same quadrature as the host path, summed in
+# another order, and against the oracle's separable projections
+@pytest.mark.gpu
+@pytest.mark.parametrize("D,k,n,scheme", [(1, 3, 5, "sparse"), (2, 3, 4, "sparse"), (3, 2, 4, "sparse"),
+                                          (2, 2, 3, "full"), (4, 2, 3, "sparse")])
+def test_vcoeffs_DG_device_matches_host(sgdg, D, k, n, scheme):
+    f = lambda p: np.sin(2 * np.pi * (p @ np.arange(1, D + 1))) * np.exp(p[:, 0]) + p[:, -1] ** 2
+    host = sgdg.vcoeffs_DG(D, k, n, f, scheme)
+    dev = sgdg.vcoeffs_DG(D, k, n, f, scheme, device=True)
+    assert np.max(np.abs(host - dev)) <= 1e-13 * np.max(np.abs(host))
+
+
+@pytest.mark.gpu
+def test_vcoeffs_DG_device_matches_oracle(sgdg, O):
+    D, k, n = 2, 3, 4
+    f = lambda p: np.sin(2 * np.pi * p[:, 0]) * np.cos(4 * np.pi * p[:, 1]) + p[:, 0] ** 2
+    got = sgdg.vcoeffs_DG(D, k, n, f, device=True)
+    s = O.vcoeffs_1d(k, n, lambda x: np.sin(2 * np.pi * x))
+    c = O.vcoeffs_1d(k, n, lambda x: np.cos(4 * np.pi * x))
+    x2 = O.vcoeffs_1d(k, n, lambda x: x ** 2)
+    one = O.vcoeffs_1d(k, n, lambda x: np.ones_like(x))
+    ref = O.tensor_construct(D, k, n, [s, c]) + O.tensor_construct(D, k, n, [x2, one])
+    assert np.max(np.abs(got - ref)) < 1e-12
