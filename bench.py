@@ -119,9 +119,13 @@ def workload_config(solves, state_dofs):
 
 
 class Clocks:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples (20 ms apart, time-stamped) from before the batch is
+    built to after the timed region; stop() keeps the samples taken inside the
+    timed region or in the 0.5 s of warm-up steps right before it (the same
+    kernel under load), since the timed region alone can be shorter than one
+    sample interval."""
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
@@ -134,12 +138,13 @@ class Clocks:
         try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """t0, t1: the timed region (time.time())."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -149,23 +154,30 @@ class Clocks:
             self.proc.kill()
         self.f.flush()
         self.f.seek(0)
-        sm, smax, reasons = [], [], set()
+        import datetime
+        sm, smax, reasons, inside = [], [], set(), 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.f.read().splitlines():
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 8:
+            if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[0]))
-                smax.append(float(parts[1]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                mhz, mx = float(parts[1]), float(parts[2])
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[4:8]):
+            if t0 is not None and not (t0 - 0.5 <= ts <= t1 + 0.05):
+                continue
+            inside += 1 if t0 is None or ts >= t0 else 0
+            sm.append(mhz)
+            smax.append(mx)
+            for nm, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         os.unlink(self.f.name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+                "samples": len(sm), "samples_in_timed_region": inside,
+                "window": "timed region and the 0.5 s of warm-up before it", "reasons": sorted(reasons)}
 
 
 def measured_peak_hbm():
@@ -526,6 +538,8 @@ def run_ours(args):
     # CUDA events below are recorded on it
     stream = torch.cuda.Stream(device=dev)
 
+    clk = Clocks(local)
+    clk.start()
     states = initial_states(sg.fourier_coeffs, args.solves, 1000 + 100000 * rank)
     b = sg.Batch()
     ids = [b.add("wave", D, K, NLEV, y0, DT) for y0 in states]
@@ -539,11 +553,10 @@ def run_ours(args):
         b.step(1)
     torch.cuda.synchronize()
 
-    clk = Clocks(local)
-    clk.start()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    tw0 = time.time()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -551,9 +564,10 @@ def run_ours(args):
         b.step(1)
     e1.record(stream)
     torch.cuda.synchronize()
+    tw1 = time.time()
     if dist:
         dist.barrier()
-    clocks = clk.stop()
+    clocks = clk.stop(tw0, tw1)
     ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     gpu_state0 = b.state(ids[0]) if rank == 0 else None
     value = job_rate(dofs_per_step, args.steps, world, ms / 1e3)
