@@ -393,7 +393,9 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     // the RK4 stage update of its state runs in place (for the wave also the
     // element's f component, whose derivative is the stage input of v).  The
     // pencils of one dimension partition the coefficients, so every state
-    // element is updated once per stage.
+    // element is updated once per stage.  The FP64 state is read and written
+    // once per stage: its accesses are evict-first, leaving L2 to the groups'
+    // partial sums and stage inputs.
     float* __restrict__ uout = C.u[in_sel ^ 1];
     constexpr int R_ = WAVE ? 2 : kOutRows;  // the wave carries two components per row
     tile_columns(W, lw, [&](int j, int r0, int rstep) {
@@ -422,11 +424,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
 #pragma unroll
             for (int u = 0; u < R_; u++) {
                 prev[u] = first ? 0.f : __ldcg(rc + off[u]);
-                yv[u] = __ldcg(C.y + bv + off[u]);
-                av[u] = stage != 1 ? __ldcg(C.acc + bv + off[u]) : 0.0;
+                yv[u] = __ldcs(C.y + bv + off[u]);
+                av[u] = stage != 1 ? __ldcs(C.acc + bv + off[u]) : 0.0;
                 if (WAVE) {
-                    yf[u] = __ldcg(C.y + b + off[u]);
-                    af[u] = stage != 1 ? __ldcg(C.acc + b + off[u]) : 0.0;
+                    yf[u] = __ldcs(C.y + b + off[u]);
+                    af[u] = stage != 1 ? __ldcs(C.acc + b + off[u]) : 0.0;
                     kf[u] = __ldcg(uin + b + C.N + off[u]);
                 }
             }
@@ -440,16 +442,16 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
                 double un;
                 rk_stage(stage, dt, hdt, dt6, f32_to_f64(v), yv[u], av[u], un);
                 if (stage == 4)
-                    __stcg(C.y + bv + o, yv[u]);
+                    __stcs(C.y + bv + o, yv[u]);
                 else
-                    __stcg(C.acc + bv + o, av[u]);
+                    __stcs(C.acc + bv + o, av[u]);
                 __stcg(uout + bv + o, f64_to_f32(un));
                 if (WAVE) {
                     rk_stage(stage, dt, hdt, dt6, f32_to_f64(kf[u]), yf[u], af[u], un);
                     if (stage == 4)
-                        __stcg(C.y + b + o, yf[u]);
+                        __stcs(C.y + b + o, yf[u]);
                     else
-                        __stcg(C.acc + b + o, af[u]);
+                        __stcs(C.acc + b + o, af[u]);
                     __stcg(uout + b + o, f64_to_f32(un));
                 }
             }
