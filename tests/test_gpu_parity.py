@@ -211,25 +211,30 @@ def test_plain_steps_for_many_solves(sgdg, O):
 
 
 def test_cfg1_advection_against_the_exact_translated_solution(sgdg, O):
-    # configuration 1 checked against the exact solution f0(x - a t): every
-    # Fourier mode keeps its wave vector and shifts its phase by -2 pi a.vel t;
-    # the projected exact solution is what a perfect integrator would give, so
-    # the GPU forms' distance to it is the DG discretisation error, equal to
-    # the FP64 oracle's own distance to it
-    D, k, n, t1 = 2, 3, 5, 1.0
+    # configuration 1's data checked against the exact solution f0(x - a t):
+    # every Fourier mode keeps its wave vector and shifts its phase by
+    # -2 pi a.vel t.  At n = 5 the sparse grid resolves the (3, 3) mode poorly
+    # and the DG error at t = 1 is 0.41; it falls 6x and 20x per level.  The
+    # GPU forms' distance to the exact solution equals the FP64 oracle's.
+    D, k, t1 = 2, 3, 1.0
     rng = np.random.default_rng(1)
     modes = []
     for _ in range(4):
         a = tuple(int(v) for v in rng.integers(1, 4, size=D))
         modes.append((a, float(rng.uniform(-1, 1)), "sin" if rng.random() < 0.5 else "cos", 0.0))
     vel = np.random.default_rng(2).uniform(-1, 1, size=D)
-    f0 = sgdg.fourier_coeffs(D, k, n, modes)
-    exact = sgdg.fourier_coeffs(D, k, n, [(a, amp, kind, ph - 2 * np.pi * float(np.dot(a, vel)) * t1)
-                                          for a, amp, kind, ph in modes])
-    ref = O.CSR(O.advection_matrix_raw(D, k, n, vel)).rk4(f0, 1e-3, 1000, nthreads=8)
-    e_oracle = rel(ref, exact)
-    for method in ("plain", "matfree"):
-        _, st = sgdg.advect_evolve(D, k, n, vel, f0, 0.0, t1, dt=1e-3, method=method)
-        e = rel(st[-1], exact)
-        print("cfg1 %s: rel L2 vs exact translated solution %.3e (oracle %.3e)" % (method, e, e_oracle))
-        assert abs(e - e_oracle) <= 1e-6 and e < 5e-2
+    errs = {"plain": [], "matfree": []}
+    for n in (5, 6, 7):
+        f0 = sgdg.fourier_coeffs(D, k, n, modes)
+        exact = sgdg.fourier_coeffs(D, k, n, [(a, amp, kind, ph - 2 * np.pi * float(np.dot(a, vel)) * t1)
+                                              for a, amp, kind, ph in modes])
+        ref = O.CSR(O.advection_matrix_raw(D, k, n, vel)).rk4(f0, 1e-3, 1000, nthreads=8)
+        e_oracle = rel(ref, exact)
+        for method in ("plain", "matfree"):
+            _, st = sgdg.advect_evolve(D, k, n, vel, f0, 0.0, t1, dt=1e-3, method=method)
+            e = rel(st[-1], exact)
+            print("n=%d %s: rel L2 vs exact translated solution %.4e (oracle %.4e)" % (n, method, e, e_oracle))
+            assert abs(e - e_oracle) <= 1e-6 * max(1.0, e_oracle)
+            errs[method].append(e)
+    for method, e in errs.items():
+        assert e[0] > 5 * e[1] > 25 * e[2], (method, e)
