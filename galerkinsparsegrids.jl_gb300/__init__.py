@@ -22,7 +22,7 @@ from . import _lib
 from ._lib import SGDGError, check, lib
 
 __all__ = [
-    "get_size", "index_map", "V2Dref", "D2Vref", "V2D", "D2V", "dg_coeffs", "vcoeffs_DG", "vcoeffs_1d",
+    "get_size", "index_map", "V2Dref", "D2Vref", "V2D", "D2V", "dg_coeffs", "vcoeffs_DG", "vcoeffs_1d", "pos_vcoeffs_DG",
     "tensor_construct", "fourier_coeffs", "periodic_DLF_matrix", "D_matrix", "grad_matrix", "laplacian_matrix",
     "SparseGridOperator", "wave_evolve", "advect_evolve", "energy_func", "Batch", "SGDGError", "set_hbm_budget",
     "hbm_in_use",
@@ -290,20 +290,57 @@ def _csr_from(nnz_fn, export_fn, m):
     return sp.csr_matrix((val[:nnz.value], col[:nnz.value], rp), shape=(m, m))
 
 
-def periodic_DLF_matrix(k, n):
-    """1D hierarchical periodic DG derivative (src/1d_derivative.jl:136-148), CSR."""
+def periodic_DLF_matrix(k, n, basis="hier"):
+    """1D periodic DG derivative (src/1d_derivative.jl:136-148), CSR: the
+    hierarchical Q' A Q or, with basis="pos", the position-basis A =
+    periodic_pos_DLF_matrix (src/1d_derivative.jl:108-111)."""
+    if basis == "pos":
+        return SparseGridOperator(1, k, n, basis="pos").csr(1)
+    if basis != "hier":
+        raise ValueError("basis must be \"hier\" or \"pos\" (nodal and point are not built)")
     L = lib()
     return _csr_from(lambda p: L.sgdg_dlf_1d_nnz(k, n, p), lambda a, b, c: L.sgdg_dlf_1d_export(k, n, a, b, c),
                      k << n)
 
 
+def pos_vcoeffs_DG(k, level, f, q=None, hmax=1.0 / 16):
+    """Position-basis coefficients of f (src/1d_dg_functions.jl:103-117): for
+    cell = 1..2^level and mode = 1..k (mode fastest) the integral of
+    basis(level, cell, mode) f over the cell, basis the orthonormal Legendre
+    polynomial of the cell (src/1d_dg_functions.jl:83-93).  The reference
+    integrates each with hquadrature; here every cell at once with a q-point
+    Gauss-Legendre rule on sub-intervals no wider than hmax.  ``f`` takes an
+    (npts, 1) array of points and returns npts values."""
+    q = q or max(8, k + 4)
+    gx, gw = np.polynomial.legendre.leggauss(q)
+    ncell = 1 << level
+    h = 1.0 / ncell
+    sub = max(1, int(np.ceil(h / hmax - 1e-12)))
+    loc = np.concatenate([(s + 0.5 + 0.5 * gx) / sub for s in range(sub)])  # in [0, 1] of a cell
+    wts = np.concatenate([0.5 * gw / sub for _ in range(sub)]) * h
+    B = np.stack([np.sqrt(2.0) * np.polynomial.polynomial.polyval(2 * loc - 1, _legendre_monomials(m))
+                  for m in range(k)]) * 2.0 ** (level / 2.0)  # (k, P), the same for every cell
+    nodes = (np.arange(ncell)[:, None] + loc[None, :]) * h
+    F = np.asarray(f(nodes.reshape(-1, 1)), np.float64).reshape(nodes.shape)
+    return np.einsum("cp,mp,p->cm", F, B, wts).ravel()
+
+
 class SparseGridOperator:
     """Device-backed derivative operators for one (D, k, n, scheme)."""
 
-    def __init__(self, D, k, n, scheme="sparse"):
-        self.D, self.k, self.n, self.scheme = D, k, n, scheme
+    def __init__(self, D, k, n, scheme="sparse", basis="hier"):
+        """basis="pos" (D = 1 only) holds the position-basis operators of
+        wave_evolve_1D; they run the plain form only."""
+        self.D, self.k, self.n, self.scheme, self.basis = D, k, n, scheme, basis
         h = ctypes.c_void_p()
-        check(lib().sgdg_op_create(D, k, n, _scheme(scheme), ctypes.byref(h)))
+        if basis == "hier":
+            check(lib().sgdg_op_create(D, k, n, _scheme(scheme), ctypes.byref(h)))
+        elif basis == "pos":
+            if D != 1:
+                raise ValueError("the position basis is one-dimensional (D = 1)")
+            check(lib().sgdg_op_create_1d(k, n, _lib.BASES["pos"], ctypes.byref(h)))
+        else:
+            raise ValueError("basis must be \"hier\" or \"pos\"")
         self._h = h
         self.N = get_size(D, k, n, scheme)
 
@@ -449,20 +486,37 @@ def norm_squared(coeffs, basis="hier"):
 
 def wave_evolve_1D(k, max_level, f0, v0, time0, time1, basis="hier", order="rk4", dt=None, nsteps=None, nout=2,
                    method="plain"):
-    """wave_evolve_1D (src/pdes.jl:89-130) in the hierarchical basis, where
-    the 1D sparse grid is the full grid and the evolution is wave_evolve(1, ...)."""
+    """wave_evolve_1D (src/pdes.jl:89-121).  basis="hier": the 1D sparse grid
+    is the full grid and the evolution is wave_evolve(1, ...).  basis="pos":
+    functions are projected with pos_vcoeffs_DG, D_op is the position-basis
+    periodic_DLF_matrix, the right-hand side is wave_data(D_op * D_op) and the
+    plain FP64 form steps it on the GPU; states are [f; v] in the position
+    basis.  The reference's "nodal" basis throws and its "point" basis is not
+    built."""
+    if basis == "pos":
+        if method != "plain":
+            raise ValueError("the position basis runs the plain form only")
+        if callable(f0):
+            f0 = pos_vcoeffs_DG(k, max_level, f0)
+        if callable(v0):
+            v0 = pos_vcoeffs_DG(k, max_level, v0)
+        op = SparseGridOperator(1, k, max_level, basis="pos")
+        return wave_evolve(1, k, max_level, f0, v0, time0, time1, order=order, dt=dt, nsteps=nsteps, nout=nout,
+                           method=method, op=op)
     if basis != "hier":
-        raise ValueError("basis: only \"hier\" is implemented on the GPU")
+        raise ValueError("basis must be \"hier\" or \"pos\" (nodal evolution throws in the reference; point is "
+                         "not built)")
     return wave_evolve(1, k, max_level, f0, v0, time0, time1, order=order, dt=dt, nsteps=nsteps, nout=nout,
                        method=method)
 
 
 def energy_func_1D(k, level, soln, basis="hier"):
     """||D u||^2 + ||u_t||^2 per stored state of a 1D solution
-    (src/pdes.jl:237-255), D the periodic hierarchical 1D operator."""
-    if basis != "hier":
-        raise ValueError("basis: only \"hier\" is implemented")
-    D_op = periodic_DLF_matrix(k, level)
+    (src/pdes.jl:237-255), D the periodic 1D operator of the basis ("hier"
+    or "pos")."""
+    if basis not in ("hier", "pos"):
+        raise NotImplementedError("nodal and point basis norms are not implemented (as in the reference)")
+    D_op = periodic_DLF_matrix(k, level, basis=basis)
     times, states = soln
     energies = []
     for st in states:

@@ -11,13 +11,14 @@ from . import build as _build
 OK, EINVAL, ENOMEM_BUDGET, ETIMEOUT, ECUDA, ECANCELLED, ENOGPU, EUNSUPPORTED, EIO, ENONFINITE = range(10)
 SCHEMES = {"sparse": 0, "full": 1}
 METHODS = {"plain": 0, "matfree": 1}
+BASES = {"hier": 0, "pos": 1}
 KIND_ADVECT, KIND_WAVE = 0, 1
 OP_LAPLACIAN, OP_WAVE_RHS = 0, -1
 
 # every symbol include/sgdg.h declares
 EXPORTS = [
     "sgdg_version", "sgdg_last_error", "sgdg_get_size", "sgdg_index_map", "sgdg_dg_coeffs", "sgdg_dlf_1d_nnz",
-    "sgdg_dlf_1d_export", "sgdg_op_create", "sgdg_op_destroy", "sgdg_op_size", "sgdg_op_nnz",
+    "sgdg_dlf_1d_export", "sgdg_op_create", "sgdg_op_create_1d", "sgdg_op_destroy", "sgdg_op_size", "sgdg_op_nnz",
     "sgdg_op_export_csr", "sgdg_op_device_nnz", "sgdg_op_export_device_csr", "sgdg_apply", "sgdg_apply_device", "sgdg_apply_noalloc", "sgdg_wave_evolve",
     "sgdg_advect_evolve", "sgdg_op_plain_steps_device", "sgdg_debug_bounds", "sgdg_vcoeffs_contract",
     "sgdg_batch_create", "sgdg_batch_destroy", "sgdg_batch_add", "sgdg_batch_remove", "sgdg_batch_set_stream",
@@ -78,6 +79,7 @@ def lib(build=True):
     _sig(L, "sgdg_dlf_1d_nnz", [_ci, _ci, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_dlf_1d_export", [_ci, _ci, _i64p, _i32p, _f64p])
     _sig(L, "sgdg_op_create", [_ci, _ci, _ci, _ci, ctypes.POINTER(_vp)])
+    _sig(L, "sgdg_op_create_1d", [_ci, _ci, _ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_op_destroy", [_vp])
     _sig(L, "sgdg_op_size", [_vp, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_op_nnz", [_vp, _ci, ctypes.POINTER(_c64)])

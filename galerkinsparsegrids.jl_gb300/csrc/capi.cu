@@ -45,6 +45,7 @@ using namespace sgdg;
 struct sgdg_op {
     SparseIndex ix;
     std::shared_ptr<const DLF1D> dlf;
+    int basis = SGDG_BASIS_HIER;  // SGDG_BASIS_POS: the 1D position-basis operators
     std::vector<std::unique_ptr<CSR>> dd;  // D_d, built on demand
     std::unique_ptr<CSR> lap, wave;
     std::map<int, std::unique_ptr<DeviceCSR>> dev;  // plain-form device copies by `which`
@@ -53,6 +54,19 @@ struct sgdg_op {
 
     const CSR& get(int which) {
         const int D = ix.D;
+        if (basis == SGDG_BASIS_POS) {
+            if (which != 1 && which != SGDG_OP_LAPLACIAN && which != SGDG_OP_WAVE_RHS)
+                throw Error(SGDG_EINVAL, "operator selector must be 1, 0 (laplacian) or -1 (wave RHS)");
+            if (!lap) {
+                dd[0].reset(new CSR());
+                lap.reset(new CSR());
+                pos_operators(ix.k, ix.n, dd[0].get(), lap.get());
+            }
+            if (which == 1) return *dd[0];
+            if (which == SGDG_OP_LAPLACIAN) return *lap;
+            if (!wave) wave.reset(new CSR(wave_rhs(*lap)));
+            return *wave;
+        }
         if (which >= 1 && which <= D) {
             if (!dd[which - 1]) dd[which - 1].reset(new CSR(assemble_dd(ix, *dlf, which - 1)));
             return *dd[which - 1];
@@ -71,7 +85,10 @@ struct sgdg_op {
     }
     const DevCSR& device(int which) {
         auto it = dev.find(which);
-        if (it == dev.end()) it = dev.emplace(which, gpu_operator(ix, *dlf, which, stream)).first;
+        if (it == dev.end())
+            it = dev.emplace(which, basis == SGDG_BASIS_POS ? to_device(get(which), stream)
+                                                            : gpu_operator(ix, *dlf, which, stream))
+                     .first;
         return it->second->d;
     }
     ~sgdg_op() {
@@ -340,6 +357,22 @@ int sgdg_op_create(int D, int k, int n, int scheme, sgdg_op** out) {
     API_END
 }
 
+int sgdg_op_create_1d(int k, int n, int basis, sgdg_op** out) {
+    API_BEGIN
+    NEED(out);
+    *out = nullptr;
+    if (basis != SGDG_BASIS_HIER && basis != SGDG_BASIS_POS)
+        throw Error(SGDG_EINVAL, "basis must be SGDG_BASIS_HIER (0) or SGDG_BASIS_POS (1)");
+    if (n < 2) throw Error(SGDG_EINVAL, "n must be >= 2");
+    auto op = std::make_unique<sgdg_op>();
+    op->ix = make_index(1, k, n, SGDG_SCHEME_SPARSE);
+    op->dlf = dlf1d(k, n);
+    op->dd.resize(1);
+    op->basis = basis;
+    *out = op.release();
+    API_END
+}
+
 int sgdg_op_destroy(sgdg_op* op) {
     API_BEGIN
     delete op;
@@ -406,6 +439,7 @@ static void apply_device_impl(sgdg_op* op, int which, int method, const double* 
         return;
     }
     if (method != SGDG_METHOD_MATFREE) throw Error(SGDG_EINVAL, "method must be PLAIN (0) or MATFREE (1)");
+    if (op->basis != SGDG_BASIS_HIER) throw Error(SGDG_EUNSUPPORTED, "the matrix-free form is hierarchical only");
     if (!(which == SGDG_OP_LAPLACIAN || (which >= 1 && which <= op->ix.D)))
         throw Error(SGDG_EUNSUPPORTED, "matrix-free apply supports which = 1..D or 0 (laplacian)");
     auto it = op->mf_apply.find(which);
@@ -546,6 +580,7 @@ static void plain_batch_steps(sgdg_op* op, int which, int64_t nsolves, double* y
 
 static void mf_evolve(sgdg_op* op, int kind, const double* a, const double* y0, int64_t len, double t0, double t1,
                       int64_t nsteps, int nout, double* times, double* states) {
+    if (op->basis != SGDG_BASIS_HIER) throw Error(SGDG_EUNSUPPORTED, "the matrix-free form is hierarchical only");
     cudaStream_t st = op_stream(op);
     MFEngine eng(st);
     SolveSpec sp{};
@@ -636,6 +671,7 @@ int sgdg_advect_evolve(sgdg_op* op, const double* a, const double* f0, double t0
     NEED(f0);
     NEED(states);
     check_evolve_args(nsteps, nout, t0, t1);
+    if (op->basis != SGDG_BASIS_HIER) throw Error(SGDG_EUNSUPPORTED, "advection is hierarchical only");
     const int64_t N = op->ix.N;
     if (method == SGDG_METHOD_PLAIN) {
         // -sum_d a_d D_d, assembled on the GPU (the same entries as add_scaled)

@@ -367,6 +367,29 @@ static DLF1D build_dlf(int k, int n) {
     return op;
 }
 
+static CSR to_csr(const Sp& A) {
+    CSR C;
+    C.m = A.m;
+    C.n = A.n;
+    C.rowptr = A.rp;
+    C.col = A.ci;
+    C.val = A.v;
+    return C;
+}
+
+// The position-basis route of wave_evolve_1D (src/pdes.jl:89-121 with
+// basis = "pos"): D_op = periodic_pos_DLF_matrix (src/1d_derivative.jl:108-111)
+// and laplac = D_op * D_op, a SpGEMM that keeps its structural zeros.
+void pos_operators(int k, int n, CSR* dop, CSR* lap) {
+    if (n < 2) throw Error(1, "n must be >= 2 (with <= 2 finest cells the reference's periodic fluxes cancel)");
+    if (n > 20) throw Error(1, "n too large");
+    basis(k);  // validates k
+    const RefBasis B(k);
+    const Sp A = transpose(neg_plus(pos_derivative(B, n), periodic_lf(B, n)));
+    if (lap) *lap = to_csr(spgemm(A, A));
+    if (dop) *dop = to_csr(A);
+}
+
 std::shared_ptr<const DLF1D> dlf1d(int k, int n) {
     static std::mutex mu;
     static std::map<std::pair<int, int>, std::shared_ptr<const DLF1D>> cache;

@@ -130,6 +130,9 @@ CSR assemble_dd(const SparseIndex& ix, const DLF1D& op, int d);  // D_matrix(D, 
 CSR spgemm_sum(const std::vector<const CSR*>& A);                  // sum_i A_i * A_i
 CSR add_scaled(const std::vector<const CSR*>& A, const std::vector<double>& s);
 CSR wave_rhs(const CSR& lap);                                                // wave_data
+// periodic_pos_DLF_matrix(k, n) and its square (the position-basis operators
+// of wave_evolve_1D); either pointer may be null
+void pos_operators(int k, int n, CSR* dop, CSR* lap);
 
 // ------------------------------------------------------ nodal transforms ----
 // Maps between the modal (hierarchical), nodal and point bases of the Vlasov

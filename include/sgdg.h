@@ -80,6 +80,18 @@ int sgdg_dlf_1d_export(int k, int n, int64_t *rowptr, int32_t *col, double *val)
  * D_matrix / grad_matrix / laplacian_matrix (src/multidim_derivative.jl:61-79).
  * Requires n >= 2 and 1 <= k <= 10. */
 int sgdg_op_create(int D, int k, int n, int scheme, sgdg_op **out);
+/* A 1D operator handle in the hierarchical basis (as sgdg_op_create(1, k, n,
+ * SGDG_SCHEME_SPARSE, out)) or in the position basis of wave_evolve_1D
+ * (src/pdes.jl:89-121, basis = "pos"): which = 1 is
+ * periodic_DLF_matrix(k, n; basis = "pos") = periodic_pos_DLF_matrix
+ * (src/1d_derivative.jl:108-111, 136-148), which = SGDG_OP_LAPLACIAN its
+ * product D_op * D_op (structural zeros kept, as SparseArrays' `*` keeps them)
+ * and SGDG_OP_WAVE_RHS wave_data around that (src/pdes.jl:22-49).  Vectors
+ * hold the k 2^n position-basis coefficients, cell-major (index (cell - 1) k
+ * + mode - 1).  The position basis runs the plain form only: the matrix-free
+ * form and advection return SGDG_EUNSUPPORTED. */
+enum { SGDG_BASIS_HIER = 0, SGDG_BASIS_POS = 1 };
+int sgdg_op_create_1d(int k, int n, int basis, sgdg_op **out);
 int sgdg_op_destroy(sgdg_op *op);
 int sgdg_op_size(const sgdg_op *op, int64_t *N);
 /* Stored entries of the assembled operator `which` (numerical zeros counted). */

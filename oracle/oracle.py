@@ -55,7 +55,7 @@ def lib():
         L.or_basis.restype = ctypes.c_double
         for name, args in [("or_hier2pos", [ctypes.c_int] * 2), ("or_pos_dlf", [ctypes.c_int] * 2),
                            ("or_dmat1d", [ctypes.c_int] * 2), ("or_dmatrix", [ctypes.c_int] * 5),
-                           ("or_laplacian", [ctypes.c_int] * 4), ("or_wave_rhs", [vp]),
+                           ("or_laplacian", [ctypes.c_int] * 4), ("or_wave_rhs", [vp]), ("or_matmul", [vp, vp]),
                            ("or_advection", [ctypes.c_int] * 4 + [_f64p]),
                            ("or_from_csc", [ctypes.c_int64] * 3 + [_i64p, _i32p, _f64p])]:
             f = getattr(L, name)
@@ -177,6 +177,15 @@ def periodic_pos_DLF_matrix(k, n):
 def periodic_DLF_matrix(k, n):
     """1D hierarchical periodic DG derivative (src/1d_derivative.jl:113-117)."""
     return _Mat(lib().or_dmat1d(k, n)).csc()
+
+
+def pos_wave_rhs_raw(k, n):
+    """wave_evolve_1D's right-hand side in the position basis
+    (src/pdes.jl:89-121, basis = "pos"): wave_data(D_op * D_op), D_op =
+    periodic_pos_DLF_matrix.  Returns (D_op, laplac, RHS) as oracle matrices."""
+    A = _Mat(lib().or_pos_dlf(k, n))
+    lap = _Mat(lib().or_matmul(A.ptr, A.ptr))
+    return A, lap, _Mat(lib().or_wave_rhs(lap.ptr))
 
 
 def D_matrix(D, d, k, n, scheme="sparse"):
@@ -316,6 +325,22 @@ def vcoeffs_1d(k, n, f, q=24):
                     vv = np.array([v(k, lvl, c, m, x) for x in xs])
                     s += float(np.sum(gw * vv * f(xs))) * 0.5 * (a1 - a0)
                 out.append(s)
+    return np.array(out)
+
+
+def pos_vcoeffs_1d(k, level, f, q=24):
+    """pos_vcoeffs_DG (src/1d_dg_functions.jl:103-117): the integral of
+    basis(level, cell, mode) * f over each cell (mode fastest), by q-point
+    Gauss-Legendre per cell (the oracle's stand-in for hquadrature)."""
+    gx, gw = np.polynomial.legendre.leggauss(q)
+    h = 1.0 / (1 << level)
+    out = []
+    for c in range(1, (1 << level) + 1):
+        xs = (c - 1) * h + 0.5 * h * (1 + gx)
+        fx = f(xs)
+        for m in range(1, k + 1):
+            bb = np.array([basis(level, c, m, x) for x in xs])
+            out.append(float(np.sum(gw * bb * fx)) * 0.5 * h)
     return np.array(out)
 
 

@@ -608,6 +608,13 @@ or_mat *or_pos_dlf(int k, int n) {
     return A;
 }
 
+/* src/pdes.jl:108-109 (wave_evolve_1D): laplac = *(D_op, D_op), SparseArrays'
+ * spmatmul, structural zeros kept */
+or_mat *or_matmul(const or_mat *A, const or_mat *B) {
+    or_init();
+    return spmatmul(A, B);
+}
+
 /* src/1d_derivative.jl:113-117: Q' * (A * Q) */
 or_mat *or_dmat1d(int k, int n) {
     or_init();

@@ -140,8 +140,8 @@ def test_norm_squared_and_energy_1d_host(sgdg, O):
     for s, e in zip(states, E):
         want = np.sum((D @ s[:n1]) ** 2) + np.sum(s[n1:] ** 2)
         assert abs(e - want) <= 1e-12 * want
-    with pytest.raises(ValueError):
-        sgdg.energy_func_1D(k, level, (times, states), basis="pos")
+    with pytest.raises(NotImplementedError):
+        sgdg.energy_func_1D(k, level, (times, states), basis="nodal")
 
 
 @pytest.mark.gpu
