@@ -253,7 +253,7 @@ def uneven_batch_leg(sg, stream, steps=50, warmup=5):
         if tuned:
             sg.set_tile_shape(d, k, w, c)
     return {"workload": "256 advection solves, D 2-3, k 2-4, n 4-7, dt 1e-3", "state_dofs": int(total),
-            "working_set_bytes": int(28 * total), "steps": steps,
+            "working_set_bytes": int(36 * total), "steps": steps,
             "default_tiles": {"value": dofs / (ms_default / 1e3), "ms_per_step": ms_default},
             "autotuned_tiles": {"value": dofs / (ms_tuned / 1e3), "ms_per_step": ms_tuned},
             "shapes_wlog_coop": shapes}
@@ -328,7 +328,7 @@ def vlasov_leg(sg, stream, steps, batch=16):
                             "roofline": {"bound": "hbm", "achieved": rate * bpd / 1e9, "peak": peak, "unit": "GB/s",
                                          "frac": rate * bpd / 1e9 / peak, "peak_kind": peak_kind,
                                          "bytes_per_dof_update": bpd,
-                                         "working_set_bytes": int(batch * N * (24 + 4 + 4 * 4 * (2 * Dx)))}}
+                                         "working_set_bytes": int(batch * N * (32 + 4 + 4 * 4 * (2 * Dx)))}}
     return out
 
 
@@ -643,7 +643,7 @@ def run_ours(args):
     if prof:
         # per-launch DRAM bytes scaled to this batch from the profiled case
         traffic = prof.get("dram_bytes_per_launch_per_solve", 0) * args.solves
-    working_set = total * (8 + 8 + 4 + 4) + args.solves * (total // args.solves // 2) * 4
+    working_set = total * (8 + 8 + 4 * 4) + args.solves * (total // args.solves // 2) * 4
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -19,8 +19,8 @@ namespace sgdg {
 // The rare inputs go through real calls: a call is not if-converted, so the
 // hardware conversion (an FP64-pipe instruction) is not issued, predicated
 // off, for every element.
-__device__ __noinline__ double f32_to_f64_rare(float f) { return (double)f; }
-__device__ __noinline__ float f64_to_f32_rare(double x) { return (float)x; }
+static __device__ __noinline__ double f32_to_f64_rare(float f) { return (double)f; }
+static __device__ __noinline__ float f64_to_f32_rare(double x) { return (float)x; }
 
 __device__ __forceinline__ double f32_to_f64(float f) {
     const unsigned u = __float_as_uint(f);

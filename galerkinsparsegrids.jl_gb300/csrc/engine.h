@@ -75,7 +75,10 @@ struct MFClass {
     const int64_t* blockoff;  // level-block offsets of every pencil of the class
     double* y;                // arenas, nslots * Ns
     double* acc;
-    float* u[2];
+    // FP32 stage inputs: stage s of a step reads u[(s - 1) % 4] and its RK
+    // update writes u[s % 4] (the fourth stage u[0], the next step's input),
+    // so within a whole-step launch no buffer is written after it was read
+    float* u[4];
     float* rhs;               // nslots * N
     const double* dt;         // per slot: dt, dt / 2, dt / 6
     const float* coef;        // per slot, 16 entries: factor on D_d as hi[8], lo[8]
@@ -115,9 +118,11 @@ struct MFItem {
     int16_t src;       // input: -1 the stage input, 0..2 a scratch vector
     int16_t dst;       // TILE_STORE / TILE_WACC output vector
     int16_t wsel;      // TILE_WACC: the weight (term) index
-    int16_t pad;
+    int16_t stage;     // RK stage 1..4 of the item in a whole-step list; 0: the launch's stage
     int32_t wait_ctr;  // counter to wait for (-1: none) ...
     int32_t wait_need; // ... until it reaches this value
+    int32_t win_ctr;   // whole-step list: counter of the RK phase that wrote the stage input (<= 0: none) ...
+    int32_t win_need;  // ... which must reach this value before the input is gathered
     int32_t done_ctr;  // counter incremented when the item is done
     int32_t lmax;      // pass: 1-based max level of the pencil along d
     int32_t lp;        // pass: log2 prod_{q<d} cells_q

@@ -31,11 +31,10 @@
 #include "bounds.cuh"
 #include "engine.h"
 #include "cvt.cuh"
+#include "mf_sweep.cuh"
 #include "rk.cuh"
 
 namespace sgdg {
-
-__device__ __forceinline__ int block_level(int rb) { return rb == 0 ? 1 : (32 - __clz(rb)) + 1; }
 
 __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
@@ -55,80 +54,6 @@ __device__ __forceinline__ int ld_relaxed(const int* p) {
     int v;
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
     return v;
-}
-
-// acc[i][c] += S(rb, cb)[i][jj] * src[cb*K + jj][jq*CPT + c] over the stored
-// blocks of row block rb with cb < nrb; S = hi + lo (two FP32 accumulators).
-struct OpTable {  // shared-memory copy of the class's 1D operator table
-    const int* rowptr;
-    const int* ent;
-    const float* val;
-};
-
-template <int K, int CPT>
-__device__ __forceinline__ void sweep(const OpTable& T, const float* __restrict__ src, int W, int nrb, int rb, int jq,
-                                      int p0, int pstep, float (&out)[K][CPT]) {
-    constexpr int RS = ((2 * K + 3) / 4) * 4;
-    float2 acc[K][CPT];
-#pragma unroll
-    for (int i = 0; i < K; i++)
-#pragma unroll
-        for (int c = 0; c < CPT; c++) acc[i][c] = make_float2(0.f, 0.f);
-    const int pb = T.rowptr[rb], pe = T.rowptr[rb + 1];
-    for (int p = pb + p0; p < pe; p += pstep) {
-        const int e = T.ent[p];
-        const int cb = e >> 12;
-        if (cb >= nrb) break;
-        float x[K][CPT];
-#pragma unroll
-        for (int jj = 0; jj < K; jj++) {
-            const float* xp = src + (cb * K + jj) * W + jq * CPT;
-            if constexpr (CPT == 4) {
-                const float4 v = *reinterpret_cast<const float4*>(xp);
-                x[jj][0] = v.x;
-                x[jj][1] = v.y;
-                x[jj][2] = v.z;
-                x[jj][3] = v.w;
-            } else {
-                const float2 v = *reinterpret_cast<const float2*>(xp);
-                x[jj][0] = v.x;
-                x[jj][1] = v.y;
-            }
-        }
-        const float4* sv = reinterpret_cast<const float4*>(T.val + (e & 4095) * (K * RS));
-#pragma unroll
-        for (int i = 0; i < K; i++) {
-            float srow[RS];
-#pragma unroll
-            for (int v = 0; v < RS / 4; v++) {
-                const float4 f = sv[i * (RS / 4) + v];
-                srow[4 * v] = f.x;
-                srow[4 * v + 1] = f.y;
-                srow[4 * v + 2] = f.z;
-                srow[4 * v + 3] = f.w;
-            }
-#pragma unroll
-            for (int jj = 0; jj < K; jj++) {
-                const float2 s = make_float2(srow[2 * jj], srow[2 * jj + 1]);
-#pragma unroll
-                for (int c = 0; c < CPT; c++) acc[i][c] = __ffma2_rn(s, make_float2(x[jj][c], x[jj][c]), acc[i][c]);
-            }
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < K; i++)
-#pragma unroll
-        for (int c = 0; c < CPT; c++) out[i][c] = acc[i][c].x + acc[i][c].y;
-}
-
-template <int K, int CPT>
-__device__ __forceinline__ void warp_sum(float (&o)[K][CPT]) {
-#pragma unroll
-    for (int i = 0; i < K; i++)
-#pragma unroll
-        for (int c = 0; c < CPT; c++)
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) o[i][c] += __shfl_xor_sync(0xffffffffu, o[i][c], off);
 }
 
 // Applies the pencil's 1D operator to src for every (row block, column quad)
@@ -189,9 +114,19 @@ __device__ __forceinline__ void tile_columns(int W, int lw, ColFn&& col) {
 // level's cell count) are tabulated once per tile in shared memory.
 constexpr int kOutRows = 4;       // rows per batch of the output loops
 
+// FP64 state loads: from L2 (never an L1 line another SM's write left stale:
+// in a whole-step launch the state was written by an earlier stage's item,
+// possibly on another SM), with an evict-first L2 policy (each value is read
+// once per stage).
+__device__ __forceinline__ double ld_state(const double* p, unsigned long long pol) {
+    double v;
+    asm volatile("ld.global.cg.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
 template <int K, int CPT, bool WAVE, bool TWICE>
 __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, int stage, int in_sel, float* smem,
-                          int* ctr, int* err, int* claim) {
+                          int* ctr, int* err, int* claim, unsigned long long pol) {
     const int tid = threadIdx.x;
     const int nrb = 1 << (it.lmax - 1);
     const int m = nrb * K;
@@ -227,12 +162,22 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
         const int cd0 = l >= 2 ? rb - (1 << (l - 2)) : 0;
         rinfo[row] = make_int2((int)C.blockoff[it.boff + l - 1] + kD * (cd0 << lp) + i * kd1, l > 2 ? l - 2 : 0);
     }
-    // an input written by the previous phase of this launch must be complete
-    if ((it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0 && tid == 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
+    // an input written by the previous phase of this launch must be complete;
+    // in a whole-step launch, so must the previous stage's RK update of the
+    // stage input
+    if (tid == 0) {
+        if (it.win_ctr > 0) wait_counter(ctr + it.win_ctr, it.win_need, err);
+        if ((it.flags & TILE_WAIT_IN) && it.wait_ctr >= 0) wait_counter(ctr + it.wait_ctr, it.wait_need, err);
+    }
     __syncthreads();
     const float* __restrict__ uin = C.u[in_sel];
     if (it.src < 0) {
-        // gather the stage input (written by the previous launch) into X
+        // gather the stage input into X.  The copies go through L1: the input
+        // was written by the previous launch or, in a whole-step launch, by
+        // the previous stage's RK update of this group (which the item waited
+        // for), and no L1 line can hold an older copy -- a stage-input buffer
+        // is read by one stage of a launch only, after it was written, and
+        // groups start on 128-byte boundaries of the buffers.
         tile_columns(W, lw, [&](int j, int r0, int rstep) {
             float* xc = X + j;
             const int s = cslot[j];
@@ -266,17 +211,26 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             const float* base = vin + (size_t)s * C.N + ca[j];
             const int bj = cb[j];
             const size_t step2 = 2 * (size_t)C.vstride;
-            for (int row = r0; row < m; row += rstep) {
-                const int2 ri = rinfo[row];
-                const int o = ri.x + (bj << ri.y);
-                if (!SGDG_IN(ca[j] + o, C.N)) {
-                    xc[row * W] = 0.f;
-                    continue;
+            // kOutRows rows' loads in flight at a time
+            for (int row0 = r0; row0 < m; row0 += kOutRows * rstep) {
+                float v[kOutRows];
+#pragma unroll
+                for (int u = 0; u < kOutRows; u++) {
+                    const int row = row0 + u * rstep;
+                    v[u] = 0.f;
+                    if (row < m) {
+                        const int2 ri = rinfo[row];
+                        const int o = ri.x + (bj << ri.y);
+                        if (SGDG_IN(ca[j] + o, C.N)) {
+                            const float* p = base + o;
+                            v[u] = __ldcg(p);
+                            for (int q = 1; q < nsum; q++) v[u] += __ldcg(p + q * step2);  // the D products, in order
+                        }
+                    }
                 }
-                const float* p = base + o;
-                float v = __ldcg(p);
-                for (int q = 1; q < nsum; q++) v += __ldcg(p + q * step2);  // the D products, in order
-                xc[row * W] = v;
+#pragma unroll
+                for (int u = 0; u < kOutRows; u++)
+                    if (row0 + u * rstep < m) xc[(row0 + u * rstep) * W] = v[u];
             }
         });
     }
@@ -396,7 +350,7 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     // element is updated once per stage.  The FP64 state is read and written
     // once per stage: its accesses are evict-first, leaving L2 to the groups'
     // partial sums and stage inputs.
-    float* __restrict__ uout = C.u[in_sel ^ 1];
+    float* __restrict__ uout = C.u[(in_sel + 1) & 3];
     constexpr int R_ = WAVE ? 2 : kOutRows;  // the wave carries two components per row
     tile_columns(W, lw, [&](int j, int r0, int rstep) {
         const int s = cslot[j];
@@ -424,11 +378,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
 #pragma unroll
             for (int u = 0; u < R_; u++) {
                 prev[u] = first ? 0.f : __ldcg(rc + off[u]);
-                yv[u] = __ldcs(C.y + bv + off[u]);
-                av[u] = stage != 1 ? __ldcs(C.acc + bv + off[u]) : 0.0;
+                yv[u] = ld_state(C.y + bv + off[u], pol);
+                av[u] = stage != 1 ? ld_state(C.acc + bv + off[u], pol) : 0.0;
                 if (WAVE) {
-                    yf[u] = __ldcs(C.y + b + off[u]);
-                    af[u] = stage != 1 ? __ldcs(C.acc + b + off[u]) : 0.0;
+                    yf[u] = ld_state(C.y + b + off[u], pol);
+                    af[u] = stage != 1 ? ld_state(C.acc + b + off[u], pol) : 0.0;
                     kf[u] = __ldcg(uin + b + C.N + off[u]);
                 }
             }
@@ -462,8 +416,8 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
 }
 
 __global__ void __launch_bounds__(kMFThreads, 3)
-    k_mf_stage(const MFItem* __restrict__ items, int nitems, const MFClass* __restrict__ classes, int* ctr, int stage,
-               int in_sel, int* err, int table_bytes) {
+    k_mf_stage(const MFItem* __restrict__ items, int nitems, const MFClass* __restrict__ classes, int* ctr, int lstage,
+               int lin_sel, int* err, int table_bytes) {
     // dynamic shared memory: [1D operator table of the current class][tile]
     extern __shared__ __align__(16) float smem[];
     float* tile = smem + table_bytes / 4;
@@ -473,6 +427,8 @@ __global__ void __launch_bounds__(kMFThreads, 3)
     __shared__ int s_cls_id;   // class in s_cls (-1: none)
     __shared__ const int32_t* s_cached;  // the table in shared memory, by its global row pointers (null: none)
     const int tid = threadIdx.x;
+    unsigned long long pol;  // L2 evict-first policy of the FP64 state streams
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
     constexpr int kItemWords = sizeof(MFItem) / 4;
     constexpr int kClsWords = sizeof(MFClass) / 4;
     static_assert(kItemWords <= 32, "item fits one warp");
@@ -546,24 +502,27 @@ __global__ void __launch_bounds__(kMFThreads, 3)
             T = OpTable{trow, tent, tval};
         }
         // Vlasov sweeps once, like advection; the wave twice unless its
-        // squared table is used
+        // squared table is used.  An item of a whole-step list carries its
+        // RK stage (stage input u[(stage - 1) % 2]).
         const int kind = C.kind != MF_KIND_WAVE ? 0 : it.tab == TABLE_SQUARE ? 1 : 2;
+        const int stage = it.stage > 0 ? it.stage : lstage;
+        const int in_sel = it.stage > 0 ? (it.stage - 1) & 3 : lin_sel;
         switch (C.k * 3 + kind) {
-            case 3: pass_tile<1, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 4: pass_tile<1, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 5: pass_tile<1, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 6: pass_tile<2, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 7: pass_tile<2, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 8: pass_tile<2, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 9: pass_tile<3, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 10: pass_tile<3, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 11: pass_tile<3, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 12: pass_tile<4, 2, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 13: pass_tile<4, 2, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 14: pass_tile<4, 2, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 15: pass_tile<5, 2, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 16: pass_tile<5, 2, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
-            case 17: pass_tile<5, 2, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item); break;
+            case 3: pass_tile<1, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 4: pass_tile<1, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 5: pass_tile<1, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 6: pass_tile<2, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 7: pass_tile<2, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 8: pass_tile<2, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 9: pass_tile<3, 4, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 10: pass_tile<3, 4, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 11: pass_tile<3, 4, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 12: pass_tile<4, 2, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 13: pass_tile<4, 2, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 14: pass_tile<4, 2, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 15: pass_tile<5, 2, false, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 16: pass_tile<5, 2, true, false>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
+            case 17: pass_tile<5, 2, true, true>(it, C, T, stage, in_sel, tile, ctr, err, &s_item, pol); break;
             default:
                 if (tid == 32) s_item = nitems;  // unreachable (k in 1..5): stop
                 break;

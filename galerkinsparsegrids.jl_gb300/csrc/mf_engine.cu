@@ -5,9 +5,10 @@
 // solves.  plan() rebuilds the arenas of classes whose solves changed (states
 // move into the new arena device-to-device), keeps the others as they are, and
 // rebuilds the ordered work list.
-// One RK4 step is four launches of k_mf_stage (one per stage) captured once in
-// a CUDA graph; a membership change drops the graph and the next step
-// re-captures it.
+// One RK4 step is one launch of k_mf_stage over a work list holding all four
+// stages (each group's stages in order, different groups' stages interleaved),
+// captured once in a CUDA graph; a membership change drops the graph and the
+// next step re-captures it.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -25,6 +26,7 @@ cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t
 cudaError_t launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t st);
 
 static constexpr size_t kWaveLag = 3;       // steps between a group's consecutive phases in the work list
+static constexpr int kStageKey = 1 << 22;   // counter keys of a whole-step list: key + (stage - 1) * kStageKey
 
 // The wave's D_d D_d on a pencil of line length lmax: one sweep of the
 // squared line operator for lmax <= kWaveSquareLevels, two sweeps of the
@@ -107,9 +109,9 @@ int MFEngine::add(const SolveSpec& sp, const double* y0, const float* weights) {
 }
 
 int64_t MFEngine::solve_bytes(int64_t N, int64_t Ns, int kind, int D) {
-    // y, acc (FP64), two stage inputs (FP32), partial sums (FP32); Vlasov:
+    // y, acc (FP64), four stage inputs (FP32), partial sums (FP32); Vlasov:
     // two scratch vectors per phase dimension and 2 D point weights (FP32)
-    return Ns * (8 + 8 + 4 + 4) + N * 4 + (kind == MF_KIND_VLASOV ? N * 4 * (4 * (int64_t)D) : 0);
+    return Ns * (8 + 8 + 4 * 4) + N * 4 + (kind == MF_KIND_VLASOV ? N * 4 * (4 * (int64_t)D) : 0);
 }
 
 int64_t MFEngine::dead_bytes() const {
@@ -257,6 +259,8 @@ void MFEngine::plan() {
             old_c->acc.release();
             old_c->u0.release();
             old_c->u1.release();
+            old_c->u2.release();
+            old_c->u3.release();
             old_c->rhs.release();
         }
         const int ns = (int)c.slots.size();
@@ -277,6 +281,10 @@ void MFEngine::plan() {
         c.acc.alloc(sizeof(double) * ns * c.Ns);
         c.u0.alloc(sizeof(float) * ns * c.Ns);
         c.u1.alloc(sizeof(float) * ns * c.Ns);
+        if (!s0.spec.apply) {  // the stage inputs of stages 3 and 4
+            c.u2.alloc(sizeof(float) * ns * c.Ns);
+            c.u3.alloc(sizeof(float) * ns * c.Ns);
+        }
         c.rhs.alloc(sizeof(float) * ns * c.N);
         const bool vlasov = s0.spec.kind == MF_KIND_VLASOV;
         if (vlasov) {
@@ -358,6 +366,8 @@ void MFEngine::plan() {
         m.acc = c.acc.as<double>();
         m.u[0] = c.u0.as<float>();
         m.u[1] = c.u1.as<float>();
+        m.u[2] = c.u2.p ? c.u2.as<float>() : m.u[0];
+        m.u[3] = c.u3.p ? c.u3.as<float>() : m.u[1];
         m.rhs = c.rhs.as<float>();
         if (s0.spec.kind == MF_KIND_WAVE && !s0.spec.apply && wave_square_levels() > 0) {
             const QTable& Q = qtab(s0.spec.k, s0.spec.n);
@@ -430,6 +440,8 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
         int depth = 0;      // longest chain of phases before it in the group
         int done_key = 0;   // counter it increments (phases of a join share one)
         int wait_key = -1;  // counter it waits for (-1: none)
+        int win_key = -1;   // whole-step list: the counter of the RK phase that wrote its stage input
+        int stage = 0;      // RK stage of its items (0: the launch's stage)
     };
     struct Group {
         std::vector<Phase> phases;
@@ -453,8 +465,16 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
             for (int d = 0; d < D; d++) dims.push_back(d);
         const int ns = (int)c.slots.size();
         const int64_t per_solve = 8 * c.N;
-        const int gs =
-            (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
+        int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
+        {
+            // groups start on 128-byte boundaries of the FP32 stage inputs (a
+            // multiple of 32 / gcd(Ns, 32) slots), so no L1 line of a stage
+            // input holds two groups' coefficients (groups reach a stage at
+            // different times within a whole-step launch)
+            int g32 = 32;
+            for (int64_t a = c.Ns; g32 > 1 && a % 2 == 0; a /= 2) g32 /= 2;
+            gs = std::min(ns, (gs + g32 - 1) / g32 * g32);
+        }
         int kDm1 = 1;
         for (int q = 0; q < D - 1; q++) kDm1 *= k;
         const int ng = (ns + gs - 1) / gs;
@@ -566,6 +586,36 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                 phase(P - 1, TRANSFORM_NODAL_TO_MODAL, cur, 0, TILE_FIRST | TILE_LAST | rk | TILE_WAIT_IN, 0, depth++, key,
                       prev);
             }
+            if (rk) {
+                // The whole RK4 step in one launch: the group's phase graph once
+                // per stage, stage s + 1 after stage s.  Every phase that
+                // gathers the stage input waits, before gathering, for the
+                // group's RK phase of the previous stage (which wrote it); the
+                // RK phase completes last within its stage, so everything of
+                // stage s precedes stage s + 1.  A group's stages thus
+                // interleave with other groups' stages instead of meeting at
+                // launch boundaries.
+                std::vector<Phase> base = std::move(grp.phases);
+                grp.phases.clear();
+                int maxd = 0, rkkey = -1;
+                for (const Phase& ph : base) {
+                    maxd = std::max(maxd, ph.depth);
+                    if (!ph.items.empty() && (ph.items[0].flags & TILE_RK)) rkkey = ph.done_key;
+                }
+                for (int st = 0; st < 4; st++)
+                    for (const Phase& ph : base) {
+                        Phase q;
+                        q.items = ph.items;
+                        for (MFItem& it : q.items) it.stage = (int16_t)(st + 1);
+                        q.stage = st + 1;
+                        q.depth = ph.depth + st * (maxd + 1);
+                        q.done_key = ph.done_key + st * kStageKey;
+                        q.wait_key = ph.wait_key >= 0 ? ph.wait_key + st * kStageKey : -1;
+                        const bool reads_input = !ph.items.empty() && ph.items[0].src < 0;
+                        if (st > 0 && reads_input) q.win_key = rkkey + (st - 1) * kStageKey;
+                        grp.phases.push_back(std::move(q));
+                    }
+            }
             groups.push_back(std::move(grp));
         }
     }
@@ -596,6 +646,8 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                     it.done_ctr = ctr_of[g].at(ph.done_key);
                     it.wait_ctr = ph.wait_key >= 0 ? ctr_of[g].at(ph.wait_key) : -1;
                     it.wait_need = ph.wait_key >= 0 ? items_of[g].at(ph.wait_key) : 0;
+                    it.win_ctr = ph.win_key >= 0 ? ctr_of[g].at(ph.win_key) : -1;
+                    it.win_need = ph.win_key >= 0 ? items_of[g].at(ph.win_key) : 0;
                     items.push_back(it);
                 }
             }
@@ -735,10 +787,9 @@ void MFEngine::capture() {
     }
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    cudaError_t err = cudaSuccess;
-    for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
-        err = launch_mf_stage(items_d_.as<MFItem>(), nitems_, classes_d_.as<MFClass>(), ctr_d_.as<int>(), nctr_, stage,
-                              (stage - 1) % 2, err_d_.as<int>(), smem_, table_bytes_, grid_, cs);
+    // the work list holds the whole RK4 step (every item carries its stage)
+    cudaError_t err = launch_mf_stage(items_d_.as<MFItem>(), nitems_, classes_d_.as<MFClass>(), ctr_d_.as<int>(),
+                                      nctr_, 1, 0, err_d_.as<int>(), smem_, table_bytes_, grid_, cs);
     cudaError_t e2 = cudaStreamEndCapture(cs, &g);
     if (own) cudaStreamDestroy(own);
     if (err != cudaSuccess || e2 != cudaSuccess) {
@@ -786,10 +837,8 @@ void MFEngine::build_chunks(int nchunks) {
         ch.ctr.alloc(sizeof(int) * (size_t)std::max(nctr, 1));
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(ch.st, cudaStreamCaptureModeThreadLocal));
-        cudaError_t err = cudaSuccess;
-        for (int stage = 1; stage <= 4 && err == cudaSuccess; stage++)
-            err = launch_mf_stage(ch.items.as<MFItem>(), ch.nitems, classes_d_.as<MFClass>(), ch.ctr.as<int>(), ch.nctr,
-                                  stage, (stage - 1) % 2, err_d_.as<int>(), smem_, table_bytes_, cgrid, ch.st);
+        cudaError_t err = launch_mf_stage(ch.items.as<MFItem>(), ch.nitems, classes_d_.as<MFClass>(), ch.ctr.as<int>(),
+                                          ch.nctr, 1, 0, err_d_.as<int>(), smem_, table_bytes_, cgrid, ch.st);
         cudaError_t e2 = cudaStreamEndCapture(ch.st, &g);
         if (err != cudaSuccess || e2 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);

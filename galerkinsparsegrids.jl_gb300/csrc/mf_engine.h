@@ -62,7 +62,7 @@ class MFEngine {
     void apply(const double* x_dev, double* y_dev);
 
     double dof_updates_per_step() const;
-    int64_t launches_per_step() const { return 4; }
+    int64_t launches_per_step() const { return 1; }  // the whole RK4 step in one launch
     int check_error();  // returns SGDG_OK or SGDG_ETIMEOUT after a bounded wait gave up
     static int64_t solve_bytes(int64_t N, int64_t Ns, int kind = MF_KIND_ADVECT, int D = 0);  // device bytes of a solve
     int64_t pending_bytes() const { return pending_bytes_; }
@@ -98,7 +98,7 @@ class MFEngine {
         std::vector<int32_t> boff_index;           // per (d, pencil): first entry in blockoff
         int64_t N = 0, Ns = 0;
         std::vector<int> slots;                    // solve id per slot
-        DevBuf y, acc, u0, u1, rhs, dt, coef, status, blockoff;
+        DevBuf y, acc, u0, u1, u2, u3, rhs, dt, coef, status, blockoff;
         DevBuf vb, vw;  // Vlasov: 2 scratch vectors per phase dimension and slot, point weights per slot
     };
 

@@ -223,7 +223,7 @@ extern "C" int sgdg_apply_noalloc(int D, int k, int n, int scheme, int which, co
         c.y = nullptr;
         c.acc = nullptr;
         c.u[0] = reinterpret_cast<float*>(base + r_u.off);
-        c.u[1] = c.u[0];
+        c.u[1] = c.u[2] = c.u[3] = c.u[0];
         c.rhs = reinterpret_cast<float*>(base + r_rhs.off);
         c.dt = reinterpret_cast<const double*>(base + r_dt.off);
         c.coef = reinterpret_cast<const float*>(base + r_coef.off);

@@ -124,7 +124,7 @@ def test_budget_makes_requests_wait_not_fail(sgdg, serving):
     free.close()
     sgdg.sync()
     base = sgdg.hbm_in_use()
-    need = 28 * y0s[0].size  # FP64 y, acc + FP32 u[2], rhs per coefficient
+    need = 36 * y0s[0].size  # FP64 y, acc + FP32 u[4], rhs per coefficient
     # room for two requests at a time (tables and work lists take < 64 KB)
     sgdg.set_hbm_budget(base + int(2.5 * need) + (64 << 10))
     try:
