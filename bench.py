@@ -231,7 +231,7 @@ def timed_steps(b, stream, steps, warmup):
 
 def uneven_batch_leg(sg, stream, steps=50, warmup=5):
     """256 independent advection solves, D in {2,3}, k in {2,3,4}, n in
-    {4..7}, one persistent launch per stage: default tile shapes, then the
+    {4..7}, one persistent launch per RK4 step: default tile shapes, then the
     autotuned ones."""
     import importlib
     sv = importlib.import_module(sg.__name__ + ".serving")
@@ -266,7 +266,7 @@ def vlasov_leg(sg, stream, steps, batch=16):
     operators on the GPU (derivatives, nodal transforms, point products), and
     the matrix-free FP32 form (pencil sweeps of the transforms, FP64 RK state)
     for one solve and for a batch of independent solves in one launch per
-    stage; the two forms' results after the same steps are compared."""
+    RK4 step; the two forms' results after the same steps are compared."""
     import importlib
     W = importlib.import_module(sg.__name__ + ".workloads")
     sv = importlib.import_module(sg.__name__ + ".serving")

@@ -769,8 +769,8 @@ def mcerr2(f, g, D, batch=50, Z=1.0, rng=None):
 # --------------------------------------------------------------- batches ----
 class Batch:
     """Independent solves of uneven (D, k, n) advanced together by the
-    matrix-free FP32/FP64 engine (one persistent launch per RK stage, one RK4
-    step replayed from a CUDA graph)."""
+    matrix-free FP32/FP64 engine (one persistent launch per RK4 step,
+    replayed from a CUDA graph)."""
 
     def __init__(self):
         h = ctypes.c_void_p()

@@ -39,11 +39,12 @@ struct DevCSR {
 //
 // Solves with equal (D, k, n, scheme, kind) form a class.  A class keeps its
 // solves' vectors in arenas (slot-major: slot s owns [s*Ns, (s+1)*Ns)), so a
-// tile may take columns from several solves.  One launch per RK stage runs an
-// ordered work list: for every group of slots, one pass per dimension (pencil
-// tiles: sweep the 1D operator, accumulate into rhs); the last pass applies the
-// RK stage update to the elements it completes.  Each phase waits for the
-// previous phase of its group.
+// tile may take columns from several solves.  One launch per RK4 step runs an
+// ordered work list: for every group of slots and every stage, one pass per
+// dimension (pencil tiles: sweep the 1D operator, accumulate into rhs); the
+// last pass applies the RK stage update to the elements it completes.  Each
+// phase waits for the previous phase of its group, and a stage's gathers wait
+// for the group's RK update of the stage before.
 enum : int { MF_KIND_ADVECT = 0, MF_KIND_WAVE = 1, MF_KIND_VLASOV = 2 };
 // TILE_RK: the pass completes the right-hand side and applies the RK4 update;
 // TILE_STORE: the result goes to a scratch vector; TILE_WACC: times a point

@@ -1,7 +1,9 @@
-// mf.cu -- the matrix-free form: one persistent launch per RK4 stage.
+// mf.cu -- the matrix-free form: one persistent launch per RK4 step (all
+// four stages), or per stage for single-stage lists (operator applications,
+// tile tuning).
 //
 // The launch walks an ordered work list (engine.h): for each group of solves
-// of a class, one pass per dimension d.  A pass item is a pencil tile: the
+// of a class and each RK stage, one pass per dimension d.  A pass item is a pencil tile: the
 // pencil's 1D prefix (m = k 2^(lmax-1) rows) times W columns taken across the
 // group's solves.  The tile is gathered into shared memory with cp.async,
 // swept with the 1D operator's k x k blocks (stored as FP32 hi + lo pairs and
@@ -19,9 +21,11 @@
 // claims its next item when the current one has passed all of its waits (at
 // the start of its output, so the claim's round trip overlaps the output),
 // and starts it right after that output.  An item of phase p waits (bounded
-// spin) until every item of phase p-1 of its group has finished; those come
-// earlier in the list, so progress never depends on a later item.  A wait
-// that runs out sets *err and the item goes on with what it has.
+// spin) until every item of phase p-1 of its group has finished, and an item
+// that gathers the stage input of stage s >= 2 first waits for its group's
+// RK phase of stage s - 1; those come earlier in the list, so progress never
+// depends on a later item.  A wait that runs out sets *err and the item goes
+// on with what it has.
 #include <cuda_runtime.h>
 
 #include <cstddef>

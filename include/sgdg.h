@@ -209,10 +209,11 @@ int sgdg_vlasov_write_h5(const sgdg_vlasov *v, const char *path, int64_t nout, c
                          const double *states);
 
 /* ---- batches of independent solves (matrix-free form) ------------------- */
-/* Many solves of uneven D, k, n advance together: each RK stage is one
- * persistent launch over the pencil tiles and RK chunks of every solve, and
- * one RK4 step is replayed from a CUDA graph.  State stays on the device
- * between calls. */
+/* Many solves of uneven D, k, n advance together: each RK4 step is one
+ * persistent launch over the pencil tiles of every solve and every stage
+ * (groups of solves reach the stages at different times; a stage waits only
+ * for its own group's previous stage), replayed from a CUDA graph.  State
+ * stays on the device between calls. */
 int sgdg_batch_create(sgdg_batch **out);
 int sgdg_batch_destroy(sgdg_batch *b);
 /* Adds a solve; y0 has N (advection) or 2N (wave: [f; v]) coefficients;
@@ -246,7 +247,7 @@ int sgdg_batch_download(sgdg_batch *b, double *y_all);
  * y_out may equal y_in), in one call that synchronises.  The batch's groups
  * of solves are split into nchunks (1..64) pipeline chunks on their own
  * streams, so one chunk's host<->device copies overlap the other chunks'
- * steps; a chunk's stage launches take one CTA per SM, so several chunks step
+ * steps; a chunk's step launch takes one CTA per SM, so several chunks step
  * side by side.  16 chunks suit a batch of a few hundred solves.  Pinned host
  * memory is needed for the copies to overlap. */
 int sgdg_batch_step_host(sgdg_batch *b, const double *y_in, double *y_out, int64_t nsteps, int nchunks);
