@@ -597,18 +597,16 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                 // launch boundaries.
                 std::vector<Phase> base = std::move(grp.phases);
                 grp.phases.clear();
-                int maxd = 0, rkkey = -1;
-                for (const Phase& ph : base) {
-                    maxd = std::max(maxd, ph.depth);
+                int rkkey = -1;
+                for (const Phase& ph : base)
                     if (!ph.items.empty() && (ph.items[0].flags & TILE_RK)) rkkey = ph.done_key;
-                }
                 for (int st = 0; st < 4; st++)
                     for (const Phase& ph : base) {
                         Phase q;
                         q.items = ph.items;
                         for (MFItem& it : q.items) it.stage = (int16_t)(st + 1);
                         q.stage = st + 1;
-                        q.depth = ph.depth + st * (maxd + 1);
+                        q.depth = ph.depth;  // within the stage (the order offsets the stages)
                         q.done_key = ph.done_key + st * kStageKey;
                         q.wait_key = ph.wait_key >= 0 ? ph.wait_key + st * kStageKey : -1;
                         const bool reads_input = !ph.items.empty() && ph.items[0].src < 0;
@@ -629,29 +627,40 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
             if (!ctr_of[g].count(ph.done_key)) ctr_of[g][ph.done_key] = nctr++;
             items_of[g][ph.done_key] += (int)ph.items.size();
         }
-    // wavefront order: a phase of depth p of group g in step g + kWaveLag p,
-    // deeper phases (older groups) first within a step, so a phase's
-    // predecessors were handed out at least kWaveLag steps earlier
-    int dmax = 0;
+    // wavefront order: a phase of depth p of stage s (0-based) of group g in
+    // step s SO + g + kWaveLag p, older stages and then deeper phases (older
+    // groups) first within a step, so a phase's predecessors were handed out
+    // at least kWaveLag steps earlier.  A stage's wavefront starts SO >=
+    // kWaveLag dmax + 1 steps after the previous one's (so a group's RK phase
+    // of stage s comes before its stage s + 1), and SO >= G, so the next
+    // stage ramps up while the previous one drains: about as many groups are
+    // in flight as in one stage's wavefront, and their vectors stay in L2.
+    int dmax = 0, nst = 1;
     for (auto& g : groups)
-        for (const Phase& ph : g.phases) dmax = std::max(dmax, ph.depth);
+        for (const Phase& ph : g.phases) {
+            dmax = std::max(dmax, ph.depth);
+            nst = std::max(nst, ph.stage);
+        }
     const size_t G = groups.size(), pmax = (size_t)dmax + 1;
-    for (size_t t = 0; t < G + kWaveLag * pmax; t++)
-        for (size_t pp = pmax; pp-- > 0;) {
-            if (t < kWaveLag * pp || t - kWaveLag * pp >= G) continue;
-            const size_t g = t - kWaveLag * pp;
-            for (const Phase& ph : groups[g].phases) {
-                if (ph.depth != (int)pp) continue;
-                for (MFItem it : ph.items) {
-                    it.done_ctr = ctr_of[g].at(ph.done_key);
-                    it.wait_ctr = ph.wait_key >= 0 ? ctr_of[g].at(ph.wait_key) : -1;
-                    it.wait_need = ph.wait_key >= 0 ? items_of[g].at(ph.wait_key) : 0;
-                    it.win_ctr = ph.win_key >= 0 ? ctr_of[g].at(ph.win_key) : -1;
-                    it.win_need = ph.win_key >= 0 ? items_of[g].at(ph.win_key) : 0;
-                    items.push_back(it);
+    const size_t SO = std::max(G, kWaveLag * (size_t)dmax + 1);
+    for (size_t t = 0; t < (size_t)(nst - 1) * SO + G + kWaveLag * pmax; t++)
+        for (int st = 0; st < nst; st++)
+            for (size_t pp = pmax; pp-- > 0;) {
+                const size_t t0 = (size_t)st * SO + kWaveLag * pp;
+                if (t < t0 || t - t0 >= G) continue;
+                const size_t g = t - t0;
+                for (const Phase& ph : groups[g].phases) {
+                    if (ph.depth != (int)pp || std::max(ph.stage, 1) != st + 1) continue;
+                    for (MFItem it : ph.items) {
+                        it.done_ctr = ctr_of[g].at(ph.done_key);
+                        it.wait_ctr = ph.wait_key >= 0 ? ctr_of[g].at(ph.wait_key) : -1;
+                        it.wait_need = ph.wait_key >= 0 ? items_of[g].at(ph.wait_key) : 0;
+                        it.win_ctr = ph.win_key >= 0 ? ctr_of[g].at(ph.win_key) : -1;
+                        it.win_need = ph.win_key >= 0 ? items_of[g].at(ph.win_key) : 0;
+                        items.push_back(it);
+                    }
                 }
             }
-        }
     int tb = 0;
     for (auto& cp : classes_) {
         const SolveSpec& sp = solves_[cp->slots[0]].spec;
