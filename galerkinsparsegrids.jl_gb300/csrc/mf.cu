@@ -3,14 +3,14 @@
 // tile tuning).
 //
 // The launch walks an ordered work list (engine.h): for each group of solves
-// of a class and each RK stage, one pass per dimension d.  A pass item is a pencil tile: the
-// pencil's 1D prefix (m = k 2^(lmax-1) rows) times W columns taken across the
-// group's solves.  The tile is gathered into shared memory with cp.async,
-// swept with the 1D operator's k x k blocks (stored as FP32 hi + lo pairs and
-// applied with the paired FMA __ffma2_rn, so the operator carries ~FP64
-// entries while the data stays FP32), and the result is added into the FP32
-// partial-sum vector rhs (L2-resident for the group, accessed with .cg so
-// other SMs' writes are seen).  For the wave (u_tt = sum_d D_d D_d u) the
+// of a class and each RK stage, one pass per dimension d.  A pass item is a
+// pencil tile: the pencil's 1D prefix (m = k 2^(lmax-1) rows) times W columns
+// taken across the group's solves.  The tile is gathered into shared memory
+// with cp.async, swept with the 1D operator's k x k blocks (stored as FP32
+// hi + lo pairs and applied with the paired FMA __ffma2_rn, so the operator
+// carries ~FP64 entries while the data stays FP32), and the result is added
+// into the FP32 partial-sum vector rhs (L2-resident for the group, accessed
+// with .cg so other SMs' writes are seen).  For the wave (u_tt = sum_d D_d D_d u) the
 // tile applies the 1D operator twice.  The last dimension's tile completes
 // the right-hand side of its elements and applies the RK stage update to
 // them in place: FP64 state, the stage combination, and the FP32 stage input
