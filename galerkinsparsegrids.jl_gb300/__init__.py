@@ -941,6 +941,14 @@ class Server:
         check(lib().sgdg_server_result(self._h, int(rid), y))
         return y
 
+    def snapshot(self, rid, size):
+        """Checkpoint of a request: (state now, steps done).  Submitting the
+        state for the remaining steps resumes the solve bit for bit."""
+        y = np.empty(int(size))
+        done = ctypes.c_int64()
+        check(lib().sgdg_server_snapshot(self._h, int(rid), y, ctypes.byref(done)))
+        return y, done.value
+
     def cancel(self, rid):
         check(lib().sgdg_server_cancel(self._h, int(rid)))
 

@@ -25,7 +25,7 @@ EXPORTS = [
     "sgdg_batch_step", "sgdg_batch_get_state", "sgdg_batch_state_size", "sgdg_batch_total_size",
     "sgdg_batch_upload", "sgdg_batch_download", "sgdg_batch_step_host", "sgdg_batch_step_info", "sgdg_batch_autotune",
     "sgdg_batch_add_vlasov",
-    "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes",
+    "sgdg_tile_shape", "sgdg_set_tile_shape", "sgdg_clear_tile_shapes", "sgdg_server_snapshot",
     "sgdg_transform_1d_nnz", "sgdg_transform_1d_export", "sgdg_transform_nnz", "sgdg_transform_export",
     "sgdg_transform_device_export",
     "sgdg_vlasov_create", "sgdg_vlasov_destroy", "sgdg_vlasov_size", "sgdg_vlasov_v_point",
@@ -123,6 +123,7 @@ def lib(build=True):
                                    ctypes.POINTER(_cd), ctypes.POINTER(_cd)])
     _sig(L, "sgdg_server_result", [_vp, _c64, _f64p])
     _sig(L, "sgdg_server_cancel", [_vp, _c64])
+    _sig(L, "sgdg_server_snapshot", [_vp, _c64, _f64p, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_server_counts", [_vp, ctypes.POINTER(_c64), ctypes.POINTER(_c64), ctypes.POINTER(_c64),
                                    ctypes.POINTER(_cd)])
     _sig(L, "sgdg_batch_autotune", [_vp, ctypes.POINTER(_ci)])

@@ -139,6 +139,25 @@ class Server {
 
     const Request& info(int64_t id) { return get(id); }
 
+    // Checkpoint of a request: its state now and the steps it has done (a
+    // queued request: its initial state and 0; a running one: the device
+    // state between ticks; a finished one: its result).  Submitting that
+    // state for the remaining steps continues the solve exactly: a solve's
+    // arithmetic does not depend on how its steps are chunked.
+    int64_t snapshot(int64_t id, double* y) {
+        Request& r = get(id);
+        if (r.state == SGDG_REQ_QUEUED) {
+            std::copy(r.y0.begin(), r.y0.end(), y);
+        } else if (r.state == SGDG_REQ_RUNNING) {
+            eng_.get_state(r.eid, y);
+        } else if (r.state == SGDG_REQ_DONE) {
+            std::copy(r.result.begin(), r.result.end(), y);
+        } else {
+            throw Error(r.code, r.msg);
+        }
+        return r.steps_done;
+    }
+
     // copies the result out and forgets the request
     void result(int64_t id, double* y) {
         Request& r = get(id);
@@ -320,6 +339,15 @@ int sgdg_server_result(sgdg_server* s, int64_t request_id, double* y) {
     NEED(s);
     NEED(y);
     s->srv->result(request_id, y);
+    API_END
+}
+
+int sgdg_server_snapshot(sgdg_server* s, int64_t request_id, double* y, int64_t* steps_done) {
+    API_BEGIN
+    NEED(s);
+    NEED(y);
+    const int64_t done = s->srv->snapshot(request_id, y);
+    if (steps_done) *steps_done = done;
     API_END
 }
 

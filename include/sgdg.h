@@ -305,6 +305,13 @@ int sgdg_server_status(sgdg_server *s, int64_t request_id, int *state, int64_t *
 /* Copies a finished request's state (N or 2N values) and forgets the request;
  * a failed or cancelled request returns its error code instead. */
 int sgdg_server_result(sgdg_server *s, int64_t request_id, double *y);
+/* Checkpoint of a request without removing it: its state now (N or 2N
+ * values; queued: the initial state, running: the state after the last
+ * tick, finished: the result) and *steps_done (may be NULL).  Submitting that
+ * state for the remaining steps resumes the solve with the same bits as an
+ * uninterrupted run.  A failed or cancelled request returns its error code.
+ * The reference has no resume (vlasov_evolve only dumps its trajectory). */
+int sgdg_server_snapshot(sgdg_server *s, int64_t request_id, double *y, int64_t *steps_done);
 /* Removes a queued or running request (its result becomes SGDG_ECANCELLED). */
 int sgdg_server_cancel(sgdg_server *s, int64_t request_id);
 /* Queue length, running requests, finished requests not yet collected, and

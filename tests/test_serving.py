@@ -165,3 +165,47 @@ def test_cancel_queued_and_running(sgdg, serving):
             srv.result(i, 1)
         assert e.value.code == 5  # SGDG_ECANCELLED
     assert srv.counts()[:2] == (0, 0)
+
+
+@pytest.mark.gpu
+def test_snapshot_and_resume_equals_uninterrupted(sgdg):
+    # checkpoint/resume of a served request: its state after some ticks,
+    # submitted again for the remaining steps, ends with the same bits as the
+    # uninterrupted solve (wave and advection, a neighbour request in the mix)
+    rng = np.random.default_rng(21)
+    for kind, D, k, n in (("wave", 3, 2, 4), ("advect", 2, 3, 5)):
+        N = sgdg.get_size(D, k, n)
+        y0 = rng.standard_normal(2 * N if kind == "wave" else N) * 1e-2
+        a = rng.uniform(-1, 1, D) if kind == "advect" else None
+        dt, nsteps = 1e-3, 23
+        other = rng.standard_normal(sgdg.get_size(2, 2, 4)) * 1e-2
+
+        full = sgdg.Server(max_chunk_steps=5)
+        i_full = full.submit(kind, D, k, n, y0, dt, nsteps, a=a)
+        full.submit("advect", 2, 2, 4, other, dt, 40, a=[0.3, -0.7])
+        while full.status(i_full)[0] != full.DONE:
+            full.tick()
+        ref = full.result(i_full, y0.size)
+        full.close()
+
+        srv = sgdg.Server(max_chunk_steps=5)
+        rid = srv.submit(kind, D, k, n, y0, dt, nsteps, a=a)
+        y_q, done_q = srv.snapshot(rid, y0.size)  # queued: the initial state
+        assert done_q == 0 and np.array_equal(y_q, y0)
+        srv.submit("advect", 2, 2, 4, other, dt, 40, a=[0.3, -0.7])
+        srv.tick()
+        srv.tick()
+        y_mid, done = srv.snapshot(rid, y0.size)
+        assert srv.status(rid)[0] == srv.RUNNING and done == 10
+        srv.cancel(rid)
+        rid2 = srv.submit(kind, D, k, n, y_mid, dt, nsteps - done, a=a)
+        while srv.status(rid2)[0] != srv.DONE:
+            srv.tick()
+        y_end, done_end = srv.snapshot(rid2, y0.size)  # finished: the result
+        assert done_end == nsteps - done
+        assert np.array_equal(srv.result(rid2, y0.size), ref)
+        assert np.array_equal(y_end, ref)
+        with pytest.raises(sgdg.SGDGError) as e:  # the cancelled request has no state to give
+            srv.snapshot(rid, y0.size)
+        assert e.value.code == 5
+        srv.close()
