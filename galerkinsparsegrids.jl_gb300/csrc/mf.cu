@@ -31,6 +31,7 @@
 #include <cstddef>
 #include <map>
 #include <mutex>
+#include <type_traits>
 
 #include "bounds.cuh"
 #include "engine.h"
@@ -356,6 +357,11 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
     // partial sums and stage inputs.
     float* __restrict__ uout = C.u[(in_sel + 1) & 3];
     constexpr int R_ = WAVE ? 2 : kOutRows;  // the wave carries two components per row
+    // the stage is a compile-time constant of the element loop (one loop per
+    // stage), so the RK4 formulas, the accumulator load and the stored
+    // vector are fixed per loop instead of decided per element
+    auto rk_loop = [&](auto stage_c) {
+    constexpr int STG = decltype(stage_c)::value;
     tile_columns(W, lw, [&](int j, int r0, int rstep) {
         const int s = cslot[j];
         if (s < 0 || __ldg(C.status + s) != 0) return;
@@ -383,10 +389,10 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             for (int u = 0; u < R_; u++) {
                 prev[u] = first ? 0.f : __ldcg(rc + off[u]);
                 yv[u] = ld_state(C.y + bv + off[u], pol);
-                av[u] = stage != 1 ? ld_state(C.acc + bv + off[u], pol) : 0.0;
+                av[u] = STG != 1 ? ld_state(C.acc + bv + off[u], pol) : 0.0;
                 if (WAVE) {
                     yf[u] = ld_state(C.y + b + off[u], pol);
-                    af[u] = stage != 1 ? ld_state(C.acc + b + off[u], pol) : 0.0;
+                    af[u] = STG != 1 ? ld_state(C.acc + b + off[u], pol) : 0.0;
                     kf[u] = __ldcg(uin + b + C.N + off[u]);
                 }
             }
@@ -398,15 +404,15 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
                 float v = fmaf(chi, z[u], clo * z[u]);
                 if (!first) v += prev[u];
                 double un;
-                rk_stage(stage, dt, hdt, dt6, f32_to_f64(v), yv[u], av[u], un);
-                if (stage == 4)
+                rk_stage(STG, dt, hdt, dt6, f32_to_f64(v), yv[u], av[u], un);
+                if (STG == 4)
                     __stcs(C.y + bv + o, yv[u]);
                 else
                     __stcs(C.acc + bv + o, av[u]);
                 __stcg(uout + bv + o, f64_to_f32(un));
                 if (WAVE) {
-                    rk_stage(stage, dt, hdt, dt6, f32_to_f64(kf[u]), yf[u], af[u], un);
-                    if (stage == 4)
+                    rk_stage(STG, dt, hdt, dt6, f32_to_f64(kf[u]), yf[u], af[u], un);
+                    if (STG == 4)
                         __stcs(C.y + b + o, yf[u]);
                     else
                         __stcs(C.acc + b + o, af[u]);
@@ -415,6 +421,13 @@ __device__ void pass_tile(const MFItem& it, const MFClass& C, const OpTable& T, 
             }
         }
     });
+    };
+    switch (stage) {
+        case 1: rk_loop(std::integral_constant<int, 1>{}); break;
+        case 2: rk_loop(std::integral_constant<int, 2>{}); break;
+        case 3: rk_loop(std::integral_constant<int, 3>{}); break;
+        default: rk_loop(std::integral_constant<int, 4>{}); break;
+    }
     }
     if (tid == 32) *claim = nxt;
 }
