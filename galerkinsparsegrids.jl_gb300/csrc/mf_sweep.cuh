@@ -1,8 +1,7 @@
-// mf_sweep.cuh -- the pencil sweep of the matrix-free form, shared by the
-// stage kernel (mf.cu, tiles gathered into shared memory) and the resident
-// kernel (mf_resident.cu, a whole solve's stage input held in shared memory).
-// Both apply a row block's stored k x k blocks in the same order with the
-// same paired FMAs, so an element's result does not depend on the kernel.
+// mf_sweep.cuh -- the pencil sweep of the matrix-free form: the stage
+// kernel (mf.cu) applies a pencil's 1D operator to a tile gathered into
+// shared memory, a row block's stored k x k blocks in table order with
+// paired FMAs, so an element's result does not depend on the tile shape.
 #pragma once
 #include <cuda_runtime.h>
 
