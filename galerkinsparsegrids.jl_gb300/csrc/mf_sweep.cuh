@@ -1,7 +1,7 @@
 // mf_sweep.cuh -- the pencil sweep of the matrix-free form: the stage
 // kernel (mf.cu) applies a pencil's 1D operator to a tile gathered into
-// shared memory, a row block's stored k x k blocks in table order with
-// paired FMAs, so an element's result does not depend on the tile shape.
+// shared memory, a row block's stored k x k blocks in table order, each
+// entry's hi and lo halves in the two lanes of a paired FMA.
 #pragma once
 #include <cuda_runtime.h>
 
