@@ -32,6 +32,7 @@ cudaError_t launch_csr_spmv_multi(const DevCSR& A, int nv, const double* x, int6
 cudaError_t launch_vlasov_points(const double* v, const double* F, const double* pt, int D, int64_t n, double* out,
                                  cudaStream_t st);
 cudaError_t launch_wait_selftest(const int* ctr, int need, int* err, cudaStream_t st);
+cudaError_t launch_convert_selftest(const double* x, int64_t n, unsigned long long* bad, cudaStream_t st);
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -1136,6 +1137,28 @@ int sgdg_selftest_bounded_wait(double* seconds) {
     if (seconds) *seconds = ms / 1e3;
     if (!err) throw Error(SGDG_ECUDA, "bounded wait self-test: the wait did not report giving up");
     throw Error(SGDG_ETIMEOUT, "bounded wait gave up as designed");
+    API_END
+}
+
+int sgdg_selftest_convert(const double* x, int64_t n, int64_t* mismatches, int64_t* first) {
+    API_BEGIN
+    require_gpu();
+    if (n < 0) throw Error(SGDG_EINVAL, "n must be >= 0");
+    if (n > 0) NEED(x);
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    DevBuf xs((size_t)(n > 0 ? n : 1) * sizeof(double));
+    DevBuf bad(2 * sizeof(unsigned long long));
+    unsigned long long out[2] = {0ull, ~0ull};
+    cudaError_t e = cudaMemcpyAsync(bad.p, out, sizeof(out), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && n > 0) e = cudaMemcpyAsync(xs.p, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_convert_selftest(xs.as<double>(), n, bad.as<unsigned long long>(), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, bad.p, sizeof(out), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) throw Error(SGDG_ECUDA, std::string("conversion self-test: ") + cudaGetErrorString(e));
+    if (mismatches) *mismatches = (int64_t)out[0];
+    if (first) *first = out[0] ? (int64_t)out[1] : -1;
     API_END
 }
 

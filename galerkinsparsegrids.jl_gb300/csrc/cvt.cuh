@@ -4,12 +4,12 @@
 // This GPU executes 2 FP64 operations per clock per SM, so a conversion on
 // the FP64 pipe costs as much as a DFMA of the RK update.  IEEE 754 binary32
 // and binary64 differ only in field widths and exponent bias (127 / 1023), so
-// for normal numbers both conversions are a few shifts and masks:
+// for normal numbers both conversions are a few integer operations:
 //   f32 -> f64: exact; exponent + 896, mantissa shifted left by 29.
 //   f64 -> f32: the top 23 mantissa bits, rounded to nearest with ties to
-//               even on the 29 dropped bits; a carry out of the mantissa
-//               increments the exponent (and reaches infinity exactly when
-//               round-to-nearest overflows).
+//               even on the 29 dropped bits by one 64-bit addition; a carry
+//               out of the mantissa increments the exponent (and reaches
+//               infinity exactly when round-to-nearest overflows).
 // Signed zeros are handled inline; subnormal, infinite and NaN inputs, and
 // f64 values outside the normal binary32 range, take the hardware conversion.
 #pragma once
@@ -23,26 +23,34 @@ static __device__ __noinline__ double f32_to_f64_rare(float f) { return (double)
 static __device__ __noinline__ float f64_to_f32_rare(double x) { return (float)x; }
 
 __device__ __forceinline__ double f32_to_f64(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    if (e - 1u >= 254u && (u << 1) != 0u) return f32_to_f64_rare(f);  // subnormal, inf, nan
-    // normal, or a signed zero (e == 0, mantissa 0)
-    const unsigned hi = (u & 0x80000000u) | (e != 0u ? ((e + 896u) << 20) | ((u >> 3) & 0x000fffffu) : 0u);
-    return __hiloint2double((int)hi, (int)(u << 29));
+    const unsigned u = __float_as_uint(f), a = u & 0x7fffffffu;
+    if (a - 0x00800000u >= 0x7f000000u) {                  // biased exponent 0 or 255
+        if (a == 0u) return __hiloint2double((int)u, 0);  // a signed zero
+        return f32_to_f64_rare(f);                         // subnormal, inf, nan
+    }
+    // exponent and mantissa move down by 3 bits (11-bit exponent field), the
+    // bias grows by 1023 - 127 = 896, the 3 low mantissa bits go to the low word
+    return __hiloint2double((int)(((a >> 3) + (896u << 20)) | (u & 0x80000000u)), (int)(u << 29));
 }
 
 __device__ __forceinline__ float f64_to_f32(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned e = (hi >> 20) & 0x7ffu;
-    if (e - 897u >= 254u) {                                // |x| < 2^-126, |x| >= 2^128, inf, nan
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    if ((hi & 0x7fffffffu) - (897u << 20) >= (254u << 20)) {  // |x| < 2^-126, |x| >= 2^128, inf, nan
         if (((hi << 1) | lo) == 0u) return __uint_as_float(hi);  // a signed zero
         return f64_to_f32_rare(x);
     }
-    unsigned r = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0x000fffffu) << 3) | (lo >> 29);
-    const unsigned rest = lo & 0x1fffffffu;  // the dropped bits; half an ulp is 2^28
-    r += (rest > 0x10000000u ? 1u : 0u) | (rest == 0x10000000u ? (r & 1u) : 0u);
-    return __uint_as_float(r);
+    // Round to nearest, ties to even, on the 29 dropped bits: adding one less
+    // than half an ulp plus the lowest kept bit carries into the kept bits
+    // exactly when rounding goes up (and a carry out of the mantissa raises
+    // the exponent, reaching infinity exactly when rounding overflows).
+    const unsigned long long b =
+        (((unsigned long long)hi << 32) | lo) + (0x0fffffffull + ((lo >> 29) & 1u));
+    // Bits 29..60 of the rounded pattern are the 23 kept mantissa bits and
+    // the low 9 bits of the exponent; subtracting 896 from that field (mod
+    // 2^9, done mod 2^32) leaves the binary32 exponent in bits 23..30 and a
+    // zero bit 31, since the exponent is 897..1151 here.
+    const unsigned r = (unsigned)(b >> 29) - (896u << 23);
+    return __uint_as_float(r | (hi & 0x80000000u));
 }
 
 // n / d for 0 <= n < 2^31 and a divisor d >= 1 fixed per work item, with

@@ -558,6 +558,33 @@ cudaError_t launch_wait_selftest(const int* ctr, int need, int* err, cudaStream_
     return cudaGetLastError();
 }
 
+// Self-test of the integer-pipe conversions against the hardware ones: for
+// each x[i], f64_to_f32(x) and, for the float x rounds to and for the float
+// whose bits are x's low word, f32_to_f64; a result that differs from the
+// hardware conversion in any bit counts in bad[0], and bad[1] keeps the
+// smallest such index.
+__global__ void k_convert_selftest(const double* __restrict__ x, int64_t n, unsigned long long* bad) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        const float hw = __double2float_rn(v);
+        bool ok = __float_as_uint(f64_to_f32(v)) == __float_as_uint(hw);
+        const float g[2] = {hw, __uint_as_float((unsigned)__double2loint(v))};
+        for (int q = 0; q < 2; q++)
+            ok = ok && __double_as_longlong(f32_to_f64(g[q])) == __double_as_longlong((double)g[q]);
+        if (!ok) {
+            atomicAdd(bad, 1ull);
+            atomicMin(bad + 1, (unsigned long long)i);
+        }
+    }
+}
+
+cudaError_t launch_convert_selftest(const double* x, int64_t n, unsigned long long* bad, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t blocks = (n + 255) / 256;
+    k_convert_selftest<<<(int)(blocks < 4096 ? blocks : 4096), 256, 0, st>>>(x, n, bad);
+    return cudaGetLastError();
+}
+
 int mf_columns_per_thread(int k) { return k <= 3 ? 4 : 2; }
 
 cudaError_t launch_mf_stage(const MFItem* items, int nitems, const MFClass* classes, int* ctr, int nctr, int stage,

@@ -358,6 +358,15 @@ int sgdg_evaluate_device(int D, int k, int n, int scheme, const double *coeffs_d
  * seconds the wait took; any other status is a failure. */
 int sgdg_selftest_bounded_wait(double *seconds);
 
+/* Self-test of the FP32 <-> FP64 conversions the stage kernel's RK update
+ * does on the integer pipes (the FP64 pipe is the scarce one): for each of
+ * the n host values x[i] the device rounds x[i] to FP32, and widens back to
+ * FP64 both the float x[i] rounds to and the float whose bits are x[i]'s low
+ * 32 bits, once by those routines and once by the hardware conversions.
+ * *mismatches counts the x[i] with a result differing in any bit, *first is
+ * the smallest such index (-1 if none). */
+int sgdg_selftest_convert(const double *x, int64_t n, int64_t *mismatches, int64_t *first);
+
 /* ---- resources ---------------------------------------------------------- */
 /* Upper bound on device bytes the library may hold (0 = no limit). */
 int sgdg_set_hbm_budget(int64_t bytes);
