@@ -34,7 +34,7 @@ EXPORTS = [
     "sgdg_server_create", "sgdg_server_destroy", "sgdg_server_set_stream", "sgdg_server_clock",
     "sgdg_server_submit", "sgdg_server_tick", "sgdg_server_status", "sgdg_server_result", "sgdg_server_cancel",
     "sgdg_server_counts",
-    "sgdg_evaluate", "sgdg_evaluate_device", "sgdg_tensor_sum", "sgdg_selftest_bounded_wait", "sgdg_selftest_convert", "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
+    "sgdg_evaluate", "sgdg_evaluate_device", "sgdg_tensor_sum", "sgdg_selftest_bounded_wait", "sgdg_selftest_convert", "sgdg_worklist_dryrun", "sgdg_set_hbm_budget", "sgdg_hbm_in_use", "sgdg_sync",
 ]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
 
@@ -114,6 +114,7 @@ def lib(build=True):
     _sig(L, "sgdg_tensor_sum", [_ci, _ci, _ci, _ci, _ci, _f64p, _f64p, _f64p])
     _sig(L, "sgdg_selftest_bounded_wait", [ctypes.POINTER(_cd)])
     _sig(L, "sgdg_selftest_convert", [_f64p, _c64, ctypes.POINTER(_c64), ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_worklist_dryrun", [_ci, _vp, _ci, _vp, _c64, ctypes.POINTER(_c64), ctypes.POINTER(_ci), _vp, _vp, _c64, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_server_destroy", [_vp])
     _sig(L, "sgdg_server_set_stream", [_vp, _vp])

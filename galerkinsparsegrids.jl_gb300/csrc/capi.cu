@@ -1140,6 +1140,85 @@ int sgdg_selftest_bounded_wait(double* seconds) {
     API_END
 }
 
+int sgdg_worklist_dryrun(int nclasses, const int* spec, int pass_only, int64_t* items, int64_t items_cap,
+                         int64_t* nitems, int* nctr, int64_t* classes, int64_t* blockoff, int64_t boff_cap,
+                         int64_t* nboff) {
+    API_BEGIN
+    NEED(spec);
+    NEED(nitems);
+    NEED(nboff);
+    if (nclasses < 1 || nclasses > 4096) throw Error(SGDG_EINVAL, "nclasses must be in 1..4096");
+    struct Host {
+        std::vector<std::vector<Pencil>> pencils;
+        std::vector<int32_t> boff_index;
+        std::vector<int64_t> boff;
+    };
+    std::vector<Host> host(nclasses);
+    std::vector<WLClass> cls;
+    for (int c = 0; c < nclasses; c++) {
+        const int* q = spec + 8 * c;
+        const int kind = q[0], D = q[1], k = q[2], n = q[3], scheme = q[4], ns = q[5], apply = q[6], adim = q[7];
+        if (kind != MF_KIND_ADVECT && kind != MF_KIND_WAVE && kind != MF_KIND_VLASOV)
+            throw Error(SGDG_EINVAL, "kind must be 0 (advection), 1 (wave) or 2 (Vlasov)");
+        if (D < 1 || D > 8 || k < 1 || k > 5) throw Error(SGDG_EUNSUPPORTED, "matrix-free form supports D <= 8, k <= 5");
+        if (ns < 1) throw Error(SGDG_EINVAL, "a class needs at least one solve");
+        if (apply && (adim < -1 || adim >= D)) throw Error(SGDG_EINVAL, "apply dimension out of range");
+        if (kind == MF_KIND_VLASOV && (apply || D % 2 != 0))
+            throw Error(SGDG_EINVAL, "a Vlasov solve has an even phase-space dimension and steps");
+        dlf1d(k, n);  // validates n
+        const SparseIndex ix = make_index(D, k, n, scheme);
+        Host& h = host[c];
+        for (int d = 0; d < D; d++) {
+            h.pencils.push_back(make_pencils(ix, d));
+            for (auto& pc : h.pencils.back()) {
+                h.boff_index.push_back((int32_t)h.boff.size());
+                for (auto o : pc.blockoff) h.boff.push_back(o);
+            }
+        }
+        const int64_t Ns = kind == MF_KIND_WAVE && !apply ? 2 * ix.N : ix.N;
+        if ((int64_t)ns * Ns >= (int64_t(1) << 31))
+            throw Error(SGDG_EUNSUPPORTED, "a class of solves holds more than 2^31 coefficients");
+        cls.push_back(WLClass{kind, D, k, n, apply != 0, apply ? adim : -1, ix.N, Ns, ns, h.pencils, h.boff_index});
+    }
+    std::vector<MFItem> list;
+    int nc = 0;
+    mf_work_list(cls, list, nc, pass_only != 0, nullptr, 0, 1, nullptr);
+    int64_t nb = 0;
+    for (auto& h : host) nb += (int64_t)h.boff.size();
+    *nitems = (int64_t)list.size();
+    *nboff = nb;
+    if (nctr) *nctr = nc;
+    if (items && items_cap >= (int64_t)list.size()) {
+        for (size_t i = 0; i < list.size(); i++) {
+            const MFItem& it = list[i];
+            const int64_t f[SGDG_WL_FIELDS] = {it.cls,      it.d,        it.tab,      it.flags,    it.src,
+                                               it.dst,      it.wsel,     it.stage,    it.wait_ctr, it.wait_need,
+                                               it.win_ctr,  it.win_need, it.done_ctr, it.lmax,     it.lp,
+                                               it.boff,     it.R,        it.g0,       it.W,        it.Wv,
+                                               it.kd1,      it.kDm1,     it.rlong,    it.rmagic,   it.rshift};
+            std::copy(f, f + SGDG_WL_FIELDS, items + i * SGDG_WL_FIELDS);
+        }
+    }
+    if (classes) {
+        int64_t first = 0;
+        for (int c = 0; c < nclasses; c++) {
+            classes[4 * c] = cls[c].N;
+            classes[4 * c + 1] = cls[c].Ns;
+            classes[4 * c + 2] = cls[c].nslots;
+            classes[4 * c + 3] = first;
+            first += (int64_t)host[c].boff.size();
+        }
+    }
+    if (blockoff && boff_cap >= nb) {
+        int64_t o = 0;
+        for (auto& h : host) {
+            std::copy(h.boff.begin(), h.boff.end(), blockoff + o);
+            o += (int64_t)h.boff.size();
+        }
+    }
+    API_END
+}
+
 int sgdg_selftest_convert(const double* x, int64_t n, int64_t* mismatches, int64_t* first) {
     API_BEGIN
     require_gpu();

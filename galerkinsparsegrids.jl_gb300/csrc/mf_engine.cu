@@ -432,9 +432,9 @@ void MFEngine::plan() {
 // so when a phase is handed out, its predecessor was handed out a whole
 // wavefront earlier and is normally complete: CTAs rarely wait, while the
 // groups in flight (about one per phase) keep their reused vectors in L2.
-void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only,
-                           const std::map<std::pair<int, int>, MFTile>* shapes, int chunk, int nchunks,
-                           std::vector<std::array<int, 3>>* ranges) {
+size_t mf_work_list(const std::vector<WLClass>& cls, std::vector<MFItem>& items, int& nctr, bool pass_only,
+                    const std::map<std::pair<int, int>, MFTile>* shapes, int chunk, int nchunks,
+                    std::vector<std::array<int, 3>>* ranges) {
     struct Phase {
         std::vector<MFItem> items;
         int depth = 0;      // longest chain of phases before it in the group
@@ -448,9 +448,9 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
     };
     std::vector<Group> groups;
     size_t smem = 64;
-    for (size_t ci = 0; ci < classes_.size(); ci++) {
-        ClassArena& c = *classes_[ci];
-        const SolveSpec& sp = solves_[c.slots[0]].spec;
+    for (size_t ci = 0; ci < cls.size(); ci++) {
+        const WLClass& c = cls[ci];
+        const WLClass& sp = c;
         const int D = sp.D, k = sp.k;
         const int cpt = mf_columns_per_thread(k);
         MFTile tile = mf_tile(D, k);
@@ -463,7 +463,7 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
             dims.push_back(sp.apply_dim);
         else
             for (int d = 0; d < D; d++) dims.push_back(d);
-        const int ns = (int)c.slots.size();
+        const int ns = c.nslots;
         const int64_t per_solve = 8 * c.N;
         int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ns, kGroupReuseBytes / std::max<int64_t>(1, per_solve)));
         {
@@ -661,6 +661,19 @@ void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only
                     }
                 }
             }
+    return smem;
+}
+
+void MFEngine::build_items(std::vector<MFItem>& items, int& nctr, bool pass_only,
+                           const std::map<std::pair<int, int>, MFTile>* shapes, int chunk, int nchunks,
+                           std::vector<std::array<int, 3>>* ranges) {
+    std::vector<WLClass> cls;
+    for (auto& cp : classes_) {
+        const SolveSpec& sp = solves_[cp->slots[0]].spec;
+        cls.push_back(WLClass{sp.kind, sp.D, sp.k, sp.n, sp.apply, sp.apply_dim, cp->N, cp->Ns,
+                              (int)cp->slots.size(), cp->pencils, cp->boff_index});
+    }
+    size_t smem = mf_work_list(cls, items, nctr, pass_only, shapes, chunk, nchunks, ranges);
     int tb = 0;
     for (auto& cp : classes_) {
         const SolveSpec& sp = solves_[cp->slots[0]].spec;

@@ -23,6 +23,27 @@ struct SolveSpec {
     int apply_dim = -1;         // apply mode: 0-based dimension, or -1 for the sum over all
 };
 
+// A class of solves as the work list sees it: host metadata only, so the
+// list can be built (and checked) without a GPU.
+struct WLClass {
+    int kind, D, k, n;
+    bool apply;
+    int apply_dim;
+    int64_t N, Ns;
+    int nslots;
+    const std::vector<std::vector<Pencil>>& pencils;  // per dimension
+    const std::vector<int32_t>& boff_index;           // per (d, pencil): first entry in the class's blockoff
+};
+
+// Builds the matrix-free work list of the classes -- the whole RK4 step (four
+// stages) for classes that step, one pass per dimension for classes that
+// only apply or when pass_only -- with chunk / nchunks and ranges as for
+// MFEngine::step_host; nctr receives the number of counters.  Returns the
+// shared memory a tile needs (without the operator table).
+size_t mf_work_list(const std::vector<WLClass>& cls, std::vector<MFItem>& items, int& nctr, bool pass_only,
+                    const std::map<std::pair<int, int>, MFTile>* shapes, int chunk, int nchunks,
+                    std::vector<std::array<int, 3>>* ranges);
+
 class MFEngine {
    public:
     explicit MFEngine(cudaStream_t st = nullptr) : stream_(st) {}

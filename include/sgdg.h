@@ -358,6 +358,27 @@ int sgdg_evaluate_device(int D, int k, int n, int scheme, const double *coeffs_d
  * seconds the wait took; any other status is a failure. */
 int sgdg_selftest_bounded_wait(double *seconds);
 
+/* Dry run of the matrix-free work list (host only, no GPU needed): the item
+ * list that a batch holding nclasses classes of solves would launch, for
+ * checking the schedule and the tiles' index arithmetic.  spec holds 8 ints per
+ * class: kind (0 advection, 1 wave, 2 Vlasov), D, k, n, scheme, solves, apply
+ * (0: RK4 steps, so the list holds the whole step's four stages; 1: one
+ * application) and the applied dimension (-1: the sum over all).  pass_only
+ * builds one pass per dimension without the RK update.  *nitems and *nboff
+ * receive the list's length and the total level-block offsets; when items
+ * (capacity items_cap records of SGDG_WL_FIELDS int64) and blockoff (boff_cap)
+ * are large enough they receive the records -- cls, d, tab, flags, src, dst,
+ * wsel, stage, wait_ctr, wait_need, win_ctr, win_need, done_ctr, lmax, lp, boff,
+ * R, g0, W, Wv, kd1, kDm1, rlong, rmagic, rshift, as the device items hold
+ * them -- and every class's level-block offsets one after another; classes
+ * (4 int64 per class, may be NULL) receives N, Ns, solves and the class's first
+ * index in blockoff; *nctr (may be NULL) the number of counters.  The tile
+ * shapes are the process-wide ones (sgdg_set_tile_shape). */
+#define SGDG_WL_FIELDS 25
+int sgdg_worklist_dryrun(int nclasses, const int *spec, int pass_only, int64_t *items, int64_t items_cap,
+                         int64_t *nitems, int *nctr, int64_t *classes, int64_t *blockoff, int64_t boff_cap,
+                         int64_t *nboff);
+
 /* Self-test of the FP32 <-> FP64 conversions the stage kernel's RK update
  * does on the integer pipes (the FP64 pipe is the scarce one): for each of
  * the n host values x[i] the device rounds x[i] to FP32, and widens back to
