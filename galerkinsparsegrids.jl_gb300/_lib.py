@@ -114,7 +114,7 @@ def lib(build=True):
     _sig(L, "sgdg_tensor_sum", [_ci, _ci, _ci, _ci, _ci, _f64p, _f64p, _f64p])
     _sig(L, "sgdg_selftest_bounded_wait", [ctypes.POINTER(_cd)])
     _sig(L, "sgdg_selftest_convert", [_f64p, _c64, ctypes.POINTER(_c64), ctypes.POINTER(_c64)])
-    _sig(L, "sgdg_worklist_dryrun", [_ci, _vp, _ci, _vp, _c64, ctypes.POINTER(_c64), ctypes.POINTER(_ci), _vp, _vp, _c64, ctypes.POINTER(_c64)])
+    _sig(L, "sgdg_worklist_dryrun", [_ci, _vp, _ci, _ci, _ci, _vp, _c64, ctypes.POINTER(_c64), ctypes.POINTER(_ci), _vp, _vp, _c64, ctypes.POINTER(_c64)])
     _sig(L, "sgdg_server_create", [_ci, ctypes.POINTER(_vp)])
     _sig(L, "sgdg_server_destroy", [_vp])
     _sig(L, "sgdg_server_set_stream", [_vp, _vp])

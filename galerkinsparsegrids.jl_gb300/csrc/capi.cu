@@ -1140,7 +1140,8 @@ int sgdg_selftest_bounded_wait(double* seconds) {
     API_END
 }
 
-int sgdg_worklist_dryrun(int nclasses, const int* spec, int pass_only, int64_t* items, int64_t items_cap,
+int sgdg_worklist_dryrun(int nclasses, const int* spec, int pass_only, int chunk, int nchunks, int64_t* items,
+                         int64_t items_cap,
                          int64_t* nitems, int* nctr, int64_t* classes, int64_t* blockoff, int64_t boff_cap,
                          int64_t* nboff) {
     API_BEGIN
@@ -1148,6 +1149,8 @@ int sgdg_worklist_dryrun(int nclasses, const int* spec, int pass_only, int64_t* 
     NEED(nitems);
     NEED(nboff);
     if (nclasses < 1 || nclasses > 4096) throw Error(SGDG_EINVAL, "nclasses must be in 1..4096");
+    if (nchunks < 1 || nchunks > 64 || chunk < 0 || chunk >= nchunks)
+        throw Error(SGDG_EINVAL, "chunk must be in 0..nchunks-1, nchunks in 1..64");
     struct Host {
         std::vector<std::vector<Pencil>> pencils;
         std::vector<int32_t> boff_index;
@@ -1182,7 +1185,7 @@ int sgdg_worklist_dryrun(int nclasses, const int* spec, int pass_only, int64_t* 
     }
     std::vector<MFItem> list;
     int nc = 0;
-    mf_work_list(cls, list, nc, pass_only != 0, nullptr, 0, 1, nullptr);
+    mf_work_list(cls, list, nc, pass_only != 0, nullptr, chunk, nchunks, nullptr);
     int64_t nb = 0;
     for (auto& h : host) nb += (int64_t)h.boff.size();
     *nitems = (int64_t)list.size();

@@ -364,7 +364,9 @@ int sgdg_selftest_bounded_wait(double *seconds);
  * class: kind (0 advection, 1 wave, 2 Vlasov), D, k, n, scheme, solves, apply
  * (0: RK4 steps, so the list holds the whole step's four stages; 1: one
  * application) and the applied dimension (-1: the sum over all).  pass_only
- * builds one pass per dimension without the RK update.  *nitems and *nboff
+ * builds one pass per dimension without the RK update; chunk of nchunks
+ * selects the list of one pipeline chunk of sgdg_batch_step_host (each class's
+ * groups cut into nchunks runs; 0 of 1 is the whole list).  *nitems and *nboff
  * receive the list's length and the total level-block offsets; when items
  * (capacity items_cap records of SGDG_WL_FIELDS int64) and blockoff (boff_cap)
  * are large enough they receive the records -- cls, d, tab, flags, src, dst,
@@ -375,7 +377,8 @@ int sgdg_selftest_bounded_wait(double *seconds);
  * index in blockoff; *nctr (may be NULL) the number of counters.  The tile
  * shapes are the process-wide ones (sgdg_set_tile_shape). */
 #define SGDG_WL_FIELDS 25
-int sgdg_worklist_dryrun(int nclasses, const int *spec, int pass_only, int64_t *items, int64_t items_cap,
+int sgdg_worklist_dryrun(int nclasses, const int *spec, int pass_only, int chunk, int nchunks, int64_t *items,
+                         int64_t items_cap,
                          int64_t *nitems, int *nctr, int64_t *classes, int64_t *blockoff, int64_t boff_cap,
                          int64_t *nboff);
 

@@ -17,12 +17,12 @@ FIELDS = ["cls", "d", "tab", "flags", "src", "dst", "wsel", "stage", "wait_ctr",
 ADVECT, WAVE, VLASOV = 0, 1, 2
 
 
-def dryrun(sgdg, classes, pass_only=False):
+def dryrun(sgdg, classes, pass_only=False, chunk=0, nchunks=1):
     """classes: (kind, D, k, n, scheme, solves, apply, apply_dim) per class."""
     L = sgdg.lib()
     spec = np.ascontiguousarray(np.array(classes, dtype=np.int32).reshape(-1, 8))
     ni, nb, nc = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
-    args = (len(spec), spec.ctypes.data, int(pass_only))
+    args = (len(spec), spec.ctypes.data, int(pass_only), chunk, nchunks)
     assert L.sgdg_worklist_dryrun(*args, None, 0, ctypes.byref(ni), ctypes.byref(nc), None, None, 0,
                                   ctypes.byref(nb)) == 0
     items = np.zeros((ni.value, len(FIELDS)), dtype=np.int64)
@@ -82,10 +82,11 @@ def check_schedule(it, nctr):
 
 
 def check_coverage(it, spec, cls, boff):
-    """Every phase (the items sharing a counter, dimension, table and vectors)
-    covers each element of each of its group's solves exactly once."""
+    """Every phase (the items sharing a counter, dimension and vectors; the
+    wave's short and long lines of one phase use different tables) covers
+    each element of each of its group's solves exactly once."""
     n = len(it["cls"])
-    keys = np.stack([it["done_ctr"], it["d"], it["tab"], it["src"], it["dst"], it["wsel"], it["stage"]], axis=1)
+    keys = np.stack([it["done_ctr"], it["d"], it["src"], it["dst"], it["wsel"], it["stage"]], axis=1)
     phases = {}
     for i in range(n):
         phases.setdefault(tuple(keys[i]), []).append(i)
@@ -208,6 +209,42 @@ def test_worklist_dryrun_rejects_bad_specs(sgdg):
     for bad in ([(7, 2, 2, 3, 0, 1, 0, 0)], [(ADVECT, 2, 9, 3, 0, 1, 0, 0)], [(ADVECT, 2, 2, 3, 0, 0, 0, 0)],
                 [(VLASOV, 3, 2, 3, 0, 1, 0, 0)], [(ADVECT, 2, 2, 3, 0, 1, 1, 5)]):
         spec = np.ascontiguousarray(np.array(bad, dtype=np.int32).reshape(-1, 8))
-        code = L.sgdg_worklist_dryrun(1, spec.ctypes.data, 0, None, 0, ctypes.byref(ni), None, None, None, 0,
+        code = L.sgdg_worklist_dryrun(1, spec.ctypes.data, 0, 0, 1, None, 0, ctypes.byref(ni), None, None, None, 0,
                                       ctypes.byref(nb))
         assert code != 0, bad
+
+
+@pytest.mark.parametrize("nchunks", [2, 3, 16])
+def test_worklist_pipeline_chunks(sgdg, nchunks):
+    """The host-to-host step's chunk lists: each is a valid schedule of its
+    own, and together they update every element of every solve once per
+    stage (each class's groups are cut into nchunks runs)."""
+    # 100 wave solves of 18,576 coefficients per component: groups of 42 solves
+    # (6 MB of stage input and partial sums each), so the chunks hold groups
+    batch = [(WAVE, 3, 3, 6, 0, 100, 0, 0), (ADVECT, 2, 2, 3, 0, 9, 0, 0)]
+    hits = None
+    nonempty = 0
+    for ch in range(nchunks):
+        it, spec, cls, boff, nctr = dryrun(sgdg, batch, chunk=ch, nchunks=nchunks)
+        if hits is None:
+            hits = {(c, st): np.zeros(int(cls[c][2] * cls[c][0]), dtype=np.int64)
+                    for c in range(len(spec)) for st in (1, 2, 3, 4)}
+        if len(it["cls"]) == 0:
+            continue
+        nonempty += 1
+        check_schedule(it, nctr)
+        check_coverage(it, spec, cls, boff)
+        check_stages(it)
+        for i in np.nonzero((it["flags"] & TILE_RK) != 0)[0]:
+            c = int(it["cls"][i])
+            s, o = tile_elements(it, i, spec[c], cls[c], boff)
+            np.add.at(hits[(c, int(it["stage"][i]))], s * int(cls[c][0]) + o, 1)
+    for key, h in hits.items():
+        assert np.all(h == 1), key
+    assert nonempty == min(nchunks, 3)  # the wave class's three groups, the advection class's one
+
+
+def test_worklist_groups(sgdg):
+    it, spec, cls, boff, nctr = dryrun(sgdg, [(WAVE, 3, 3, 6, 0, 100, 0, 0)])
+    firsts = sorted({int(it["done_ctr"][i]) for i in range(len(it["cls"]))})
+    assert len(firsts) == nctr - 1
