@@ -180,9 +180,9 @@ __device__ __forceinline__ void csr_rk_update(const CsrRK& rk, int64_t row, doub
 
 // the rows of bin `bin`, 2^bin = VS lanes each
 template <int VS, int NV, int W, bool RK>
-__device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, const double* __restrict__ x, int64_t xi,
+__device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, int64_t rb, const double* __restrict__ x, int64_t xi,
                                         int64_t xs, double* y, int64_t yi, int64_t ys, const CsrRK& rk) {
-    const int64_t t = (int64_t)(blockIdx.x - A.bin_block[bin]) * blockDim.x + threadIdx.x;
+    const int64_t t = (rb - A.bin_block[bin]) * blockDim.x + threadIdx.x;
     const int64_t idx = t / VS, first = A.bin_first[bin];
     const int lane = int(t % VS);
     int64_t row = idx < A.bin_first[bin + 1] - first ? (int64_t)A.bin_rows[first + idx] : -1;
@@ -203,27 +203,45 @@ __device__ __forceinline__ void csr_bin(const DevCSR& A, int bin, const double* 
     }
 }
 
-// blockIdx.y selects one of several solves sharing A (RK only): its vectors
-// sit bs elements after the previous solve's
+// With nb > 1 solves sharing A (RK only; solve s's vectors at s * bs), block
+// b is (row block, solve): the solves go in groups of sg, and within a group
+// the solve index runs fastest, so the group's passes over a row block run
+// side by side and read its matrix entries from L2 while the group's vectors
+// stay there too (A is streamed once per group instead of once per solve).
 template <int NV, int W, bool RK>
 __global__ void __launch_bounds__(256) k_csr(DevCSR A, const double* __restrict__ x, int64_t xi, int64_t xs,
-                                             double* y, int64_t yi, int64_t ys, CsrRK rk, int64_t bs) {
+                                             double* y, int64_t yi, int64_t ys, CsrRK rk, int64_t bs, int64_t nb,
+                                             int sg) {
+    int64_t rb = blockIdx.x;
     if constexpr (RK) {
-        const int64_t o = (int64_t)blockIdx.y * bs;
-        x += o;
-        y += o;
-        rk.acc += o;
-        rk.uout += o;
+        if (nb > 1) {
+            const int64_t nrb = A.bin_block[kCsrBins], b = blockIdx.x, full = nb / sg, fb = full * nrb * sg;
+            int64_t sl;
+            if (b < fb) {
+                const int64_t g = b / (nrb * sg), r = b - g * nrb * sg;
+                rb = r / sg;
+                sl = g * sg + r % sg;
+            } else {
+                const int64_t tail = nb - full * sg, r = b - fb;
+                rb = r / tail;
+                sl = full * sg + r % tail;
+            }
+            const int64_t o = sl * bs;
+            x += o;
+            y += o;
+            rk.acc += o;
+            rk.uout += o;
+        }
     }
     int bin = 0;
-    while (bin + 1 < kCsrBins && (int)blockIdx.x >= A.bin_block[bin + 1]) bin++;
+    while (bin + 1 < kCsrBins && rb >= A.bin_block[bin + 1]) bin++;
     switch (bin) {
-        case 0: csr_bin<1, NV, W, RK>(A, 0, x, xi, xs, y, yi, ys, rk); break;
-        case 1: csr_bin<2, NV, W, RK>(A, 1, x, xi, xs, y, yi, ys, rk); break;
-        case 2: csr_bin<4, NV, W, RK>(A, 2, x, xi, xs, y, yi, ys, rk); break;
-        case 3: csr_bin<8, NV, W, RK>(A, 3, x, xi, xs, y, yi, ys, rk); break;
-        case 4: csr_bin<16, NV, W, RK>(A, 4, x, xi, xs, y, yi, ys, rk); break;
-        default: csr_bin<32, NV, W, RK>(A, 5, x, xi, xs, y, yi, ys, rk); break;
+        case 0: csr_bin<1, NV, W, RK>(A, 0, rb, x, xi, xs, y, yi, ys, rk); break;
+        case 1: csr_bin<2, NV, W, RK>(A, 1, rb, x, xi, xs, y, yi, ys, rk); break;
+        case 2: csr_bin<4, NV, W, RK>(A, 2, rb, x, xi, xs, y, yi, ys, rk); break;
+        case 3: csr_bin<8, NV, W, RK>(A, 3, rb, x, xi, xs, y, yi, ys, rk); break;
+        case 4: csr_bin<16, NV, W, RK>(A, 4, rb, x, xi, xs, y, yi, ys, rk); break;
+        default: csr_bin<32, NV, W, RK>(A, 5, rb, x, xi, xs, y, yi, ys, rk); break;
     }
 }
 
@@ -340,7 +358,7 @@ template <int NV, int W, bool RK>
 static void csr_pass(const DevCSR& A, const double* x, int64_t xi, int64_t xs, double* y, int64_t yi, int64_t ys,
                      const CsrRK& rk, cudaStream_t st) {
     if (A.bin_block[kCsrBins] > 0)
-        k_csr<NV, W, RK><<<A.bin_block[kCsrBins], 256, 0, st>>>(A, x, xi, xs, y, yi, ys, rk, 0);
+        k_csr<NV, W, RK><<<A.bin_block[kCsrBins], 256, 0, st>>>(A, x, xi, xs, y, yi, ys, rk, 0, 1, 1);
     if (A.nlong > 0) {
         k_csr_segments<NV, W><<<grid_for(A.nseg * 32), 256, 0, st>>>(A, x, xi, xs);
         k_csr_long_rows<<<grid_for(A.nlong * NV), 256, 0, st>>>(A, NV, y, yi, ys, rk, RK);
@@ -389,15 +407,24 @@ cudaError_t launch_csr_rk4(const DevCSR& A, const double* uin, double* y, double
     return cudaGetLastError();
 }
 
+// solves per group of the batched row kernel: 16 solves of the 3D k=3 n=7 wave
+// (733 KB of state each) keep their vectors in L2 while they share A's rows;
+// 1, 4, 8, 32 and 64 measured 33.0, 32.0, 31.9, 31.8 and 31.8 ms per step of
+// 256 solves against 31.9 (the FP64 additions, not A's bytes, bound the pass)
+constexpr int kPlainSolveGroup = 16;
+
 // One RK4 stage of nb solves that share A, their vectors one after another
-// (solve s at s * bs): the row kernel with one grid row per solve; a matrix
-// with long rows (segment partials) takes one pass per solve.
+// (solve s at s * bs): one launch of the row kernel over (row block, solve)
+// pairs, the solves in groups that stream A once each; a matrix with long
+// rows (segment partials) takes one pass per solve.
 cudaError_t launch_csr_rk4_batch(const DevCSR& A, int64_t nb, int64_t bs, const double* uin, double* y, double* acc,
                                  double* uout, double dt, int stage, cudaStream_t st) {
     const CsrRK rk{acc, uout, dt, 0.5 * dt, dt / 6.0, stage};
-    if (A.nlong == 0 && nb <= 65535) {
-        if (A.bin_block[kCsrBins] > 0 && nb > 0)
-            k_csr<1, 1, true><<<dim3(A.bin_block[kCsrBins], (unsigned)nb), 256, 0, st>>>(A, uin, 1, 0, y, 1, 0, rk, bs);
+    const int64_t nrb = A.bin_block[kCsrBins];
+    if (A.nlong == 0 && nb * nrb < (int64_t(1) << 31)) {
+        if (nrb > 0 && nb > 0)
+            k_csr<1, 1, true><<<(unsigned)(nrb * nb), 256, 0, st>>>(A, uin, 1, 0, y, 1, 0, rk, bs, nb,
+                                                                   kPlainSolveGroup);
         return cudaGetLastError();
     }
     for (int64_t s = 0; s < nb; s++) {
