@@ -21,17 +21,24 @@ struct DeviceCSR {
 constexpr int64_t kCsrSplit = 2048;  // entries a row group sums directly
 
 // bin of a row of L <= kCsrSplit entries: the fewest lanes 2^b (up to 32)
-// that give each lane at most eight entries (fewer lanes per row: fewer FP64
-// additions in the lane reduction, which on GB300 cost as much as the FMAs)
-inline int csr_bin(int64_t L) {
+// that give each lane at most `per_lane` entries (fewer lanes per row: fewer
+// FP64 additions in the lane reduction, which on GB300 cost as much as the
+// FMAs).  32 entries per lane suit single-vector passes: the 256-solve wave
+// batch steps in 20.1 ms against 26.2 at 16 and 31.8 at 8 (its rows hold ~96
+// entries); the nodal transforms, passed over four vectors at once, keep 8
+// (the Vlasov plain step 2.60 ms against 2.66 at 16 and 2.67 at 32).
+constexpr int kCsrLaneEntries = 32;
+constexpr int kCsrLaneEntriesMulti = 8;
+inline int csr_bin(int64_t L, int per_lane) {
     int b = 0;
-    while (b + 1 < kCsrBins && (int64_t(8) << b) < L) b++;
+    while (b + 1 < kCsrBins && (int64_t(per_lane) << b) < L) b++;
     return b;
 }
 
 // Fills D.d from D's buffers (already holding rowptr, col, val for m rows)
 // and builds the long-row segments from the host copy of the row pointers.
-inline void finish_device_csr(DeviceCSR& D, const std::vector<int64_t>& rowptr, int64_t m, cudaStream_t st) {
+inline void finish_device_csr(DeviceCSR& D, const std::vector<int64_t>& rowptr, int64_t m, cudaStream_t st,
+                              int per_lane = kCsrLaneEntries) {
     const int64_t nnz = rowptr[m];
     D.d.m = m;
     D.d.nnz = nnz;
@@ -43,7 +50,7 @@ inline void finish_device_csr(DeviceCSR& D, const std::vector<int64_t>& rowptr, 
     std::vector<int64_t> cnt(kCsrBins + 1, 0);
     for (int64_t r = 0; r < m; r++) {
         const int64_t L = rowptr[r + 1] - rowptr[r];
-        if (L <= kCsrSplit) cnt[csr_bin(L) + 1]++;
+        if (L <= kCsrSplit) cnt[csr_bin(L, per_lane) + 1]++;
     }
     int64_t blocks = 0;
     for (int b = 0; b < kCsrBins; b++) {
@@ -60,7 +67,7 @@ inline void finish_device_csr(DeviceCSR& D, const std::vector<int64_t>& rowptr, 
         std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
         for (int64_t r = 0; r < m; r++) {
             const int64_t L = rowptr[r + 1] - rowptr[r];
-            if (L <= kCsrSplit) rows[(size_t)fill[csr_bin(L)]++] = (int32_t)r;
+            if (L <= kCsrSplit) rows[(size_t)fill[csr_bin(L, per_lane)]++] = (int32_t)r;
         }
     }
     D.d.bin_rows = nullptr;
@@ -109,7 +116,8 @@ inline std::unique_ptr<DeviceCSR> to_device(const CSR& A, cudaStream_t st) {
 // The plain-form operators assembled on the GPU (gpu_assemble.cu): which =
 // 1..D for D_d, SGDG_OP_LAPLACIAN, SGDG_OP_WAVE_RHS; the same stored entries
 // and values as the host assembly (assemble.cpp).
-std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st);
+std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st,
+                                        int per_lane = kCsrLaneEntries);
 // sum_d s[d] D_d over the union of patterns (the plain advection operator)
 std::unique_ptr<DeviceCSR> gpu_scaled_sum(const SparseIndex& ix, const DLF1D& dlf, const double* s, cudaStream_t st);
 // The D-dim restricted Kronecker product of the 1D transform T1 (the same

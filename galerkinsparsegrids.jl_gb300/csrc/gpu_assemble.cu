@@ -644,20 +644,21 @@ std::unique_ptr<DeviceCSR> gpu_transform(const SparseIndex& ix, const CSR& T1, c
         CK(cudaGetLastError());
     }
     CK(cudaStreamSynchronize(st));
-    finish_device_csr(*R, rph, ix.N, st);
+    finish_device_csr(*R, rph, ix.N, st, kCsrLaneEntriesMulti);  // the transforms take four vectors a pass
     return R;
 }
 
 SGDG_BOUNDS_READER(asm_bounds_violations)
 
-std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st) {
+std::unique_ptr<DeviceCSR> gpu_operator(const SparseIndex& ix, const DLF1D& dlf, int which, cudaStream_t st,
+                                        int per_lane) {
     require_gpu();
     const int D = ix.D;
     std::vector<int64_t> rp;
     if (which >= 1 && which <= D) {
         const LineTables T = line_tables(dlf, dlf.n + 1, false);
         auto A = line_operator(ix, T, which - 1, st, rp);
-        finish_device_csr(*A, rp, ix.N, st);
+        finish_device_csr(*A, rp, ix.N, st, per_lane);
         return A;
     }
     if (which != SGDG_OP_LAPLACIAN && which != SGDG_OP_WAVE_RHS)
